@@ -1,0 +1,307 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300-native electrostatic placement loop.
+
+A "step" is one Placement::step (src/placement.rs:180-228) of the plain FP32
+path on the 1,000,000-cell synthetic workload (1,050,000 nets, 16 macros,
+4,000 IO pins, 1024x1024 bins, target density 1.0), replayed from the
+context's captured CUDA graph.  `value` is Nesterov iterations/s with the
+design resident in HBM; `e2e` is the same metric through the drop-in
+host-coordinate call erp_step_host (pinned host x/y copied in and out every
+step).  `--impl reference` times the CPU restatement of the reference loop
+(the oracle, reference FP32 mode) on the machine's host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "iters/s @1M cells, jobs/h, p99 latency: mixed/batched vs plain FP32 @HPWL±0.5%"
+UNIT = "iters/s"
+L2_BYTES = 129 * 2 ** 20
+
+# Algorithmic bytes per launch of each stage (FP32 = 4 B, index = 4 B,
+# int64 = 8 B; each array counted once): N movable cells, P pins, E nets,
+# B = m*n bins.
+ALG_BYTES = {
+    "wirelength": lambda N, P, E, B: 40 * P + 4 * E + 20 * N,
+    "density": lambda N, P, E, B: 28 * N + 8 * B,
+    "spectral": lambda N, P, E, B: 12 * B + 12 * B,
+    "force": lambda N, P, E, B: 36 * N + 8 * B,
+    "nesterov": lambda N, P, E, B: 76 * N,
+    "scheduler": lambda N, P, E, B: 0,
+}
+# DRAM bytes per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum),
+# filled from the committed profiles/ summaries; None until captured.
+NCU_TRAFFIC = {}
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                  "sw_power_cap"), parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def allreduce_max(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def make_workload(name):
+    import reda_erplacer_gb300 as R
+    if name == "large":
+        d, cfg = R.workload_large()
+        desc = "plain FP32, 1,000,000 movable cells / 1,050,000 nets / 16 macros / 4,000 IO, 1024x1024 bins"
+    else:
+        d, cfg = R.workload_small()
+        desc = "plain FP32, 20,000 movable cells / 21,000 nets / 400 IO, 256x256 bins"
+    return d, cfg, desc
+
+
+def cpu_sample(d, cfg, iters, literal):
+    """Time `iters` oracle steps (all host threads) after one untimed step."""
+    from oracle import erp_oracle as O
+    m, n = cfg["bins"]
+    o = O.Oracle(d, m, n, target_density=cfg["target_density"],
+                 density_mode=O.DENSITY_REFERENCE if literal else O.DENSITY_FIXED,
+                 reduce_fp64=0 if literal else 1, num_threads=0)
+    o.step()
+    t0 = time.perf_counter()
+    for _ in range(iters):
+        o.step()
+    dt = time.perf_counter() - t0
+    o.close()
+    return iters / dt, dt
+
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return 0
+    d, cfg, desc = make_workload(args.workload)
+    iters = max(1, min(args.steps, args.ref_steps))
+    for _ in range(max(0, min(args.warmup, 1))):
+        pass
+    v, dt = cpu_sample(d, cfg, iters, literal=True)
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+        "steps": iters, "warmup": 1, "ms_per_step": 1000.0 * dt / iters,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": desc, "bins": list(cfg["bins"])},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{iters} full iterations of the workload after 1 untimed "
+                                   f"iteration; reference FP32 mode (sequential / atomic density)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    world, rank, local = dist_setup()
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    import __graft_entry__ as G
+    G.build_product()
+    import reda_erplacer_gb300 as R
+
+    d, cfg, desc = make_workload(args.workload)
+    m, n = cfg["bins"]
+    stream = torch.cuda.Stream()
+    pl = R.Placement(d, (m, n), cfg["target_density"], device=local, stream=stream.cuda_stream)
+    for _ in range(args.warmup):
+        pl.step(stats=False)
+    pl.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        pl.step(stats=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms_local = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    ms = allreduce_max(ms_local, world)
+    sc = pl.scalars()
+    st = pl.scalars()
+    x_h, y_h = pl.positions()
+    value = world * args.steps / (ms / 1000.0)
+
+    # end to end through the drop-in host-coordinate call, pinned buffers
+    N = d.num_nodes
+    xp = torch.from_numpy(x_h).pin_memory()
+    yp = torch.from_numpy(y_h).pin_memory()
+    xa, ya = xp.numpy(), yp.numpy()
+    e2e_steps = max(3, min(args.steps, 50))
+    pl.step_host(xa, ya)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        last = pl.step_host(xa, ya)
+    torch.cuda.synchronize()
+    e2e_s = allreduce_max(time.perf_counter() - t0, world)
+    e2e_value = world * e2e_steps / e2e_s
+    h2d = 8 * N
+    d2h = 8 * N + 256
+
+    # roofline of the dominant stage (isolated launches, L2 flushed)
+    stages = pl.profile_stages(reps=args.profile_reps)
+    dom = max((k for k in stages if k != "scheduler"), key=lambda k: stages[k])
+    B = m * n
+    alg = {k: ALG_BYTES[k](d.num_movable, d.num_pins, d.num_nets, B) for k in stages}
+    peak, peak_kind = measured_peak_gbs()
+    achieved = alg[dom] / (stages[dom] * 1e-3) / 1e9
+    traffic = NCU_TRAFFIC.get((args.workload, dom))
+    per_stage = {k: {"ms": stages[k], "alg_bytes": alg[k],
+                     "gbs": (alg[k] / (stages[k] * 1e-3) / 1e9) if stages[k] > 0 else None}
+                 for k in stages}
+    pl.close()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": desc, "cells": d.num_movable, "nets": d.num_nets,
+                   "pins": d.num_pins, "bins": [m, n], "target_density": cfg["target_density"],
+                   "start": "reference rule (die centre)", "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (per-step working set > 129 MiB), no flush",
+                   "iteration_after": sc["iteration"], "hpwl_after": sc["hpwl_current"],
+                   "overflow_after": sc["overflow_current"]},
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": e2e_steps, "call": "erp_step_host"},
+        "gpu_launches": int(st["graph_kernels"]) * args.steps,
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "alg_bytes": alg[dom], "ms": stages[dom]},
+        "stages": per_stage,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, dt = cpu_sample(d, cfg, args.cpu_iters, literal=False)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{args.cpu_iters} full iterations of the same workload "
+                                          f"(oracle, OpenMP, all host threads), {dt:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["large", "small"], default="large")
+    ap.add_argument("--profile-reps", type=int, default=10)
+    ap.add_argument("--cpu-iters", type=int, default=3)
+    ap.add_argument("--ref-steps", type=int, default=10)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

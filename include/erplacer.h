@@ -1,0 +1,256 @@
+/*
+ * erplacer.h — C ABI of the GB300-native (sm_103a) electrostatic global-placement
+ * loop, a drop-in for ERPlacer's (giammirove/reda-erplacer) placement step.
+ *
+ * One context = one placement design resident on one GPU.  All compute runs in
+ * hand-written CUDA kernels on the context's stream; there is no CPU fallback:
+ * every entry point fails with ERP_ECUDA / ERP_ENODEV when no usable GPU is
+ * present.  Host arrays passed in are copied; the caller keeps ownership.
+ * Calls on one context must come from one host thread at a time.
+ *
+ * Each entry point names the reference function it replaces (file:line in the
+ * reference crate).  The reference functions are `pub(crate)` Rust; the Rust
+ * binding a maintainer adds (extern "C" block + build.rs) is in INTEGRATION.md.
+ */
+#ifndef ERPLACER_H
+#define ERPLACER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ERP_ABI_VERSION 1
+
+typedef enum erp_status {
+    ERP_OK = 0,
+    ERP_EINVAL = 1,     /* bad argument or design (message in erp_last_error) */
+    ERP_ENOMEM = 2,     /* device or host allocation failed */
+    ERP_ECUDA = 3,      /* CUDA runtime error */
+    ERP_ENAN = 4,       /* non-finite value detected in positions or gradients */
+    ERP_ETIMEDOUT = 5,  /* a bounded device wait ran out */
+    ERP_ENOTSUP = 6,    /* feature not supported for these parameters */
+    ERP_ENODEV = 7,     /* no CUDA device of compute capability 10.3 */
+    ERP_ESTATE = 8      /* call not valid in the current state */
+} erp_status;
+
+/* Placement database, structure-of-arrays + CSR (the fields of reda-db's
+ * DB<T> that the loop reads; semantics restated from their use sites):
+ *  - instances: movable first (src/placement.rs:125); (x, y) lower-left DEF
+ *    coordinates; fixed IO pins are zero-size instances;
+ *  - num_pins_f: per-instance pin count stored as float (src/nesterov.rs:78);
+ *  - pins: offsets from the owning instance's lower-left corner
+ *    (src/hpwl.rs:107); pin_inst maps a pin to its instance;
+ *  - nets: CSR over pin ids; the first n_2nets nets have exactly two pins
+ *    (src/hpwl.rs:159,173);
+ *  - inst_pin_ptr / inst_pins: per-instance pin lists (macro_2_pins);
+ *  - the die spans [0, die_w] x [0, die_h] (src/nesterov.rs:131). */
+typedef struct erp_design {
+    int32_t num_nodes;
+    int32_t num_movable;
+    int32_t num_pins;
+    int32_t num_nets;
+    int32_t n_2nets;
+    int32_t _pad;
+    const float *x, *y;
+    const float *w, *h;
+    const float *num_pins_f;
+    const float *pin_ox, *pin_oy;
+    const int32_t *pin_inst;
+    const int32_t *net_ptr;
+    const int32_t *net_pins;
+    const int32_t *inst_pin_ptr;
+    const int32_t *inst_pins;
+    float die_w, die_h;
+    float cell_utilization;   /* default target density (src/placement.rs:134) */
+    float movable_area;       /* overflow normaliser (src/epotential.rs:277) */
+} erp_design;
+
+typedef enum erp_start_mode {
+    ERP_START_CENTER = 0,     /* reference rule: movable cells at the die centre (src/placement.rs:109-139) */
+    ERP_START_DB = 1          /* keep the design's coordinates (e.g. a jittered start) */
+} erp_start_mode;
+
+typedef enum erp_precision {
+    ERP_PREC_FP32 = 0         /* FP32 spectral solve (FFT-based DCT/DST), the parity path */
+} erp_precision;
+
+typedef struct erp_params {
+    int32_t num_bins_x;       /* 0: 512 like the reference (src/placement.rs:50); power of two, 16..4096 */
+    int32_t num_bins_y;
+    float target_density;     /* < 0: design cell_utilization (reference rule) */
+    int32_t start_mode;       /* erp_start_mode */
+    int32_t precision;        /* erp_precision */
+    int32_t device;           /* CUDA device ordinal */
+    void *stream;             /* cudaStream_t to run on; NULL: the context creates its own */
+    int32_t flags;            /* reserved, 0 */
+} erp_params;
+
+/* One Placement::step's scalars (the reference logs these every 10
+ * iterations, src/placement.rs:213-223).  gamma and density_weight are the
+ * values the step used, before the scheduler update. */
+typedef struct erp_step_stats {
+    int32_t iteration;        /* iteration index of the step */
+    int32_t should_stop;      /* Scheduler::should_stop after the update */
+    float hpwl;
+    float overflow;
+    float density_weight;
+    float gamma;
+    float alpha;              /* Nesterov step length after the step */
+    float beta;
+} erp_step_stats;
+
+typedef struct erp_ctx erp_ctx;
+
+const char *erp_status_string(erp_status s);
+/* Last error message of a context (NULL ctx: last error of erp_create on this thread). */
+const char *erp_last_error(const erp_ctx *ctx);
+int32_t erp_abi_version(void);
+
+/* Placement::new (src/placement.rs:159-178): Bins::new, PlacementSolution::new,
+ * PotentialComputation::new (incl. the fixed-cell initial density map),
+ * HpwlComputation::new, Scheduler::new, Nesterov::new. */
+erp_status erp_create(const erp_design *design, const erp_params *params, erp_ctx **out);
+void erp_destroy(erp_ctx *ctx);
+
+/* compute_hpwl (src/hpwl.rs:139-343): WA wirelength gradient (kept on the
+ * device) and the HPWL total (FP64 reduction).  hpwl may be NULL (no sync). */
+erp_status erp_wirelength(erp_ctx *ctx, float gamma, float *hpwl);
+
+/* compute_potential (src/epotential.rs:225-374): density scatter (int64 fixed
+ * point), overflow, spectral Poisson solve, electric force.  energy may be NULL
+ * (then the potential map is skipped, as the caller discards it,
+ * src/placement.rs:185); overflow may be NULL (no sync). */
+erp_status erp_potential(erp_ctx *ctx, int32_t iteration, float *energy, float *overflow);
+
+/* Nesterov::step_adaptive (src/nesterov.rs:27-146) on the gradients of the last
+ * erp_wirelength / erp_potential calls, with the context's density weight. */
+erp_status erp_nesterov(erp_ctx *ctx, int32_t iteration);
+
+/* Scheduler::update (src/scheduler.rs:68-73) with host-supplied metrics. */
+erp_status erp_scheduler_update(erp_ctx *ctx, float hpwl, float overflow);
+/* Scheduler::should_stop (src/scheduler.rs:75-81). */
+erp_status erp_should_stop(erp_ctx *ctx, int32_t *stop);
+
+/* Placement::step (src/placement.rs:180-228): one whole iteration, replayed from
+ * a captured CUDA graph; the scheduler runs on the device.  stats may be NULL:
+ * then the call only enqueues work (no host sync). */
+erp_status erp_step(erp_ctx *ctx, erp_step_stats *stats);
+
+/* Drop-in form for a host that owns the coordinates (the reference's
+ * ps.instances, mutated by step_adaptive, src/nesterov.rs:39): copies x/y
+ * (all nodes) to the device, runs one step, copies the new x/y back. */
+erp_status erp_step_host(erp_ctx *ctx, float *x, float *y, erp_step_stats *stats);
+
+/* Run up to max_iterations steps (the CLI loop, src/main.rs:78-90), stopping
+ * early once overflow <= stop_overflow (stop_overflow <= 0: never).  Returns
+ * the number of iterations run and the last step's stats. */
+erp_status erp_run(erp_ctx *ctx, int32_t max_iterations, float stop_overflow,
+                   int32_t *iterations_run, erp_step_stats *last);
+
+/* Scheduler / optimiser scalars. */
+typedef struct erp_scalars {
+    int32_t iteration;
+    float gamma, base_gamma, density_weight;
+    float alpha, beta;
+    float hpwl_initial, hpwl_current, hpwl_previous;
+    float overflow_current, overflow_previous;
+    double hpwl_last;         /* FP64 HPWL total of the last wirelength pass */
+    double overflow_last;     /* FP64 overflow of the last potential pass */
+    double energy_last;
+    int32_t fixed_shift;      /* S: movable density contributions are rint(v * 2^S) */
+    int32_t fixed_shift_init; /* S0 for the fixed-cell initial map */
+    int32_t num_bins_x, num_bins_y;
+    float bin_w, bin_h, target_density;
+    int32_t graph_kernels;    /* kernel launches in one captured Placement::step (0 before the first erp_step) */
+} erp_scalars;
+erp_status erp_get_scalars(erp_ctx *ctx, erp_scalars *out);
+erp_status erp_set_scalars(erp_ctx *ctx, int32_t iteration, float gamma, float density_weight,
+                           float alpha, float beta);
+
+/* Positions of all nodes (movable first). */
+erp_status erp_get_positions(erp_ctx *ctx, float *x, float *y);
+erp_status erp_set_positions(erp_ctx *ctx, const float *x, const float *y);
+/* Nesterov history (prev coords / prev grads) of all nodes. */
+erp_status erp_set_nesterov_history(erp_ctx *ctx, const float *prev_x, const float *prev_y,
+                                    const float *prev_gx, const float *prev_gy);
+
+/* Device arrays readable for inspection and tests (copied to host memory). */
+typedef enum erp_array {
+    ERP_ARR_WL_GRAD_X = 0,    /* float [num_nodes] hc.grad_x */
+    ERP_ARR_WL_GRAD_Y = 1,
+    ERP_ARR_DENS_GRAD_X = 2,  /* float [num_nodes] pc.grad_x */
+    ERP_ARR_DENS_GRAD_Y = 3,
+    ERP_ARR_PIN_GRAD_X = 4,   /* float [num_pins] grad_pins_x, original pin order */
+    ERP_ARR_PIN_GRAD_Y = 5,
+    ERP_ARR_DENSITY_I64 = 6,  /* int64 [m*n] movable fixed-point sums of the last potential pass */
+    ERP_ARR_DENSITY = 7,      /* float [m*n] density map scaled by 1/bin_area */
+    ERP_ARR_INITIAL = 8,      /* float [m*n] fixed-cell map x target density */
+    ERP_ARR_FIELD_X = 9,      /* float [m*n] */
+    ERP_ARR_FIELD_Y = 10,
+    ERP_ARR_POTENTIAL = 11,   /* float [m*n] (only after erp_potential with energy != NULL) */
+    ERP_ARR_PREV_X = 12,
+    ERP_ARR_PREV_Y = 13,
+    ERP_ARR_PREV_GX = 14,
+    ERP_ARR_PREV_GY = 15,
+    ERP_ARR_NET_HPWL = 16     /* float [num_nets] per-net HPWL, original net order */
+} erp_array;
+erp_status erp_get_array(erp_ctx *ctx, erp_array which, void *dst, size_t bytes);
+
+/* Block until the context's stream is idle. */
+erp_status erp_synchronize(erp_ctx *ctx);
+
+/* ---- profiling (the reference's time_it phases, src/utils.rs:106-124) ----
+ * Times each stage of one step in isolation: `reps` launches, each preceded by
+ * an L2 flush (a 256 MiB device write, untimed), bracketed by CUDA events on
+ * the context's stream.  ms_out[ERP_NUM_STAGES] receives the mean per launch.
+ * Mutates the placement state (positions, scheduler): call it after the
+ * measured run. */
+typedef enum erp_stage {
+    ERP_STAGE_WIRELENGTH = 0, /* WA nets + HPWL reduction + instance gather */
+    ERP_STAGE_DENSITY = 1,    /* map clear + density scatter */
+    ERP_STAGE_SPECTRAL = 2,   /* map conversion + overflow + Poisson solve (3 passes) */
+    ERP_STAGE_FORCE = 3,      /* electric force gather */
+    ERP_STAGE_NESTEROV = 4,   /* rescale + preconditioned gradient / Lipschitz + update */
+    ERP_STAGE_SCHEDULER = 5,
+    ERP_NUM_STAGES = 6
+} erp_stage;
+erp_status erp_profile_stages(erp_ctx *ctx, int32_t reps, float *ms_out);
+
+/* ---- standalone spectral solve (the Poisson part of compute_potential,
+ * src/epotential.rs:284-343) on device buffers, for the isolated-solve
+ * workload.  All pointers are device pointers of m*n floats; potential may be
+ * NULL. ---- */
+typedef struct erp_spectral erp_spectral;
+erp_status erp_spectral_create(int32_t m, int32_t n, float bin_w, float bin_h, int32_t precision,
+                               void *stream, erp_spectral **out);
+erp_status erp_spectral_solve(erp_spectral *sp, const float *rho_dev, float *field_x_dev,
+                              float *field_y_dev, float *potential_dev);
+void erp_spectral_destroy(erp_spectral *sp);
+
+/* ---- seeded synthetic netlists (stand-in for reda-db's read_db on the
+ * LEF/DEF benchmarks, which are not shipped) ---- */
+typedef struct erp_synth_params {
+    int64_t seed;
+    int32_t num_cells;        /* movable standard cells */
+    int32_t num_nets;
+    int32_t num_io;           /* fixed IO pins on the die boundary */
+    int32_t num_macros;       /* fixed rectangular macros */
+    float macro_area_frac;    /* each macro's share of the die area (e.g. 0.015) */
+    float utilization;        /* movable area / free area */
+    float site_w, row_h;      /* 0.2 / 2.0 um */
+    int32_t min_sites, max_sites; /* cell width range in sites (2..16) */
+    float jitter_frac;        /* start jitter sigma as a fraction of die width (0.001) */
+} erp_synth_params;
+typedef struct erp_synth erp_synth;
+erp_status erp_synth_create(const erp_synth_params *p, erp_synth **out);
+/* Fills *d with pointers into the generator's host arrays (valid until destroy). */
+erp_status erp_synth_design(const erp_synth *s, erp_design *d);
+void erp_synth_destroy(erp_synth *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

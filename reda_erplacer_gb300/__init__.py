@@ -1,0 +1,13 @@
+"""GB300-native (sm_103a) electrostatic global-placement loop: a drop-in for
+ERPlacer's (giammirove/reda-erplacer) placement step behind the C ABI of
+include/erplacer.h.  All compute runs in liberplacer_gb300.so; importing this
+package fails if the library has not been built (no fallback)."""
+from . import lib
+from .lib import ErpError
+from .design import Design, synth, workload_small, workload_large, bins_for_cells
+from .placement import Placement, SpectralSolver
+
+lib.load()
+
+__all__ = ["Design", "synth", "workload_small", "workload_large", "bins_for_cells", "Placement",
+           "SpectralSolver", "ErpError"]

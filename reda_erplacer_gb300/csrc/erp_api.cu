@@ -1,0 +1,859 @@
+// C ABI of liberplacer_gb300.so (include/erplacer.h): context set-up
+// (Placement::new, src/placement.rs:159-178), the reference's stage entry
+// points, the CUDA-graph Placement::step, the run loop and accessors.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "erp_internal.cuh"
+
+using namespace erp;
+
+struct erp_ctx {
+    Ctx c;
+};
+
+struct erp_spectral {
+    SpectralPlan p;
+    DevState *st;
+    std::string err;
+};
+
+static thread_local std::string g_create_err;
+
+extern "C" const char *erp_status_string(erp_status s) {
+    switch (s) {
+    case ERP_OK: return "ok";
+    case ERP_EINVAL: return "invalid argument";
+    case ERP_ENOMEM: return "out of memory";
+    case ERP_ECUDA: return "CUDA error";
+    case ERP_ENAN: return "non-finite value";
+    case ERP_ETIMEDOUT: return "device wait timed out";
+    case ERP_ENOTSUP: return "not supported";
+    case ERP_ENODEV: return "no sm_103 CUDA device";
+    case ERP_ESTATE: return "invalid state";
+    }
+    return "unknown";
+}
+
+extern "C" const char *erp_last_error(const erp_ctx *ctx) {
+    return ctx ? ctx->c.err.c_str() : g_create_err.c_str();
+}
+
+extern "C" int32_t erp_abi_version(void) { return ERP_ABI_VERSION; }
+
+namespace {
+
+bool pow2_ok(int v) { return v >= 16 && v <= 4096 && (v & (v - 1)) == 0; }
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t count) {
+    return cudaMalloc((void **)p, sizeof(T) * (count ? count : 1));
+}
+
+cudaError_t upload(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+    if (!bytes) return cudaSuccess;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+}
+
+int32_t fixed_shift(double total_area) {
+    int e = 0;
+    if (total_area > 0) frexp(total_area, &e);
+    int s = 61 - e;
+    return s < -64 ? -64 : (s > 100 ? 100 : s);
+}
+
+erp_status check_device(int dev, std::string &err) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        err = "no CUDA device available";
+        return ERP_ENODEV;
+    }
+    if (dev < 0 || dev >= count) {
+        err = "device ordinal out of range";
+        return ERP_EINVAL;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+        err = "cudaGetDeviceProperties failed";
+        return ERP_ECUDA;
+    }
+    if (prop.major != 10 || prop.minor != 3) {
+        char buf[128];
+        snprintf(buf, sizeof buf, "device %d is sm_%d%d; this library is built for sm_103a only", dev,
+                 prop.major, prop.minor);
+        err = buf;
+        return ERP_ENODEV;
+    }
+    if (cudaSetDevice(dev) != cudaSuccess) {
+        err = "cudaSetDevice failed";
+        return ERP_ECUDA;
+    }
+    return ERP_OK;
+}
+
+erp_status validate(const erp_design *d, std::string &err) {
+#define REQ(cond, msg)        \
+    if (!(cond)) {            \
+        err = msg;            \
+        return ERP_EINVAL;    \
+    }
+    REQ(d, "design is NULL");
+    REQ(d->num_nodes >= 0 && d->num_movable >= 0 && d->num_movable <= d->num_nodes, "bad node counts");
+    REQ(d->num_pins >= 0 && d->num_nets >= 0 && d->n_2nets >= 0 && d->n_2nets <= d->num_nets, "bad pin/net counts");
+    REQ(d->num_nodes == 0 || (d->x && d->y && d->w && d->h && d->num_pins_f), "instance arrays missing");
+    REQ(d->num_pins == 0 || (d->pin_ox && d->pin_oy && d->pin_inst), "pin arrays missing");
+    REQ(d->net_ptr && d->inst_pin_ptr, "CSR pointers missing");
+    REQ(d->die_w > 0 && d->die_h > 0, "die must have positive size");
+    REQ(d->net_ptr[0] == 0, "net_ptr[0] must be 0");
+    for (int e = 0; e < d->num_nets; ++e) REQ(d->net_ptr[e + 1] >= d->net_ptr[e], "net_ptr not monotone");
+    REQ(d->net_ptr[d->num_nets] == 0 || d->net_pins, "net_pins missing");
+    for (int e = 0; e < d->n_2nets; ++e) REQ(d->net_ptr[e + 1] - d->net_ptr[e] == 2, "first n_2nets nets must have 2 pins");
+    std::vector<char> seen(d->num_pins, 0);
+    for (int k = 0; k < d->net_ptr[d->num_nets]; ++k) {
+        int p = d->net_pins[k];
+        REQ(p >= 0 && p < d->num_pins, "net pin id out of range");
+        REQ(!seen[p], "a pin belongs to more than one net");
+        seen[p] = 1;
+    }
+    for (int p = 0; p < d->num_pins; ++p) REQ(d->pin_inst[p] >= 0 && d->pin_inst[p] < d->num_nodes, "pin_inst out of range");
+    REQ(d->inst_pin_ptr[0] == 0, "inst_pin_ptr[0] must be 0");
+    for (int i = 0; i < d->num_nodes; ++i) REQ(d->inst_pin_ptr[i + 1] >= d->inst_pin_ptr[i], "inst_pin_ptr not monotone");
+    REQ(d->inst_pin_ptr[d->num_nodes] == 0 || d->inst_pins, "inst_pins missing");
+    for (int k = 0; k < d->inst_pin_ptr[d->num_nodes]; ++k)
+        REQ(d->inst_pins[k] >= 0 && d->inst_pins[k] < d->num_pins, "inst pin id out of range");
+    for (int i = 0; i < d->num_nodes; ++i) {
+        REQ(isfinite(d->x[i]) && isfinite(d->y[i]) && d->w[i] >= 0 && d->h[i] >= 0, "non-finite or negative instance geometry");
+        for (int k = d->inst_pin_ptr[i]; k < d->inst_pin_ptr[i + 1]; ++k)
+            REQ(d->pin_inst[d->inst_pins[k]] == i, "inst_pins disagrees with pin_inst");
+    }
+    return ERP_OK;
+#undef REQ
+}
+
+void free_ctx(Ctx &c) {
+    void *ptrs[] = {c.x, c.y, c.w, c.h, c.npins, c.cw, c.ch, c.offx, c.offy, c.ratio, c.wlgx, c.wlgy,
+                    c.dgx, c.dgy, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.slot_cell, c.slot_off,
+                    c.slot_grad, c.net_ptr, c.net_hpwl, c.cell_slot_ptr, c.cell_slots, c.dmap,
+                    c.initial, c.rho, c.t1, c.tx, c.ty, c.tp, c.fx, c.fy, c.psi, c.tw_m, c.tw_n,
+                    c.ek_m, c.ek_n, c.wu, c.wv, c.partials, c.st};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (c.h_st) cudaFreeHost(c.h_st);
+    if (c.graph_ready) cudaGraphExecDestroy(c.graph);
+    if (c.own_stream && c.stream) cudaStreamDestroy(c.stream);
+    delete[] c.h_slot_of_pin;
+    delete[] c.h_net_of_internal;
+}
+
+SpectralPlan plan_of(Ctx &c) {
+    SpectralPlan p;
+    p.m = c.m; p.n = c.n; p.logm = c.logm; p.logn = c.logn;
+    p.bin_w = c.bin_w; p.bin_h = c.bin_h;
+    p.tw_m = c.tw_m; p.tw_n = c.tw_n; p.ek_m = c.ek_m; p.ek_n = c.ek_n;
+    p.wu = c.wu; p.wv = c.wv;
+    p.t1 = c.t1; p.tx = c.tx; p.ty = c.ty; p.tp = c.tp;
+    p.partials = c.partials; p.st = c.st; p.stream = c.stream;
+    return p;
+}
+
+}  // namespace
+
+namespace erp {
+void launch_spectral(Ctx &c, bool zero_map, bool store_rho, bool want_psi) {
+    SpectralArgs a;
+    a.dmap = c.dmap;
+    a.initial = c.initial;
+    a.fixed_inv = c.fixed_inv;
+    a.coef = c.target_density * c.bin_area;           // src/epotential.rs:272-273
+    a.inv_bin_area = c.inv_bin_area;
+    a.movable_area = (double)c.movable_area;
+    a.zero_map = zero_map;
+    a.rho_out = store_rho ? c.rho : nullptr;
+    a.fx = c.fx;
+    a.fy = c.fy;
+    a.psi = want_psi ? c.psi : nullptr;
+    a.partials = c.partials;
+    a.st = c.st;
+    launch_spectral_plan(plan_of(c), a);
+}
+}  // namespace erp
+
+#define CK(expr)                                                               \
+    do {                                                                       \
+        cudaError_t _e = (expr);                                               \
+        if (_e != cudaSuccess) {                                               \
+            c.err = std::string(#expr) + ": " + cudaGetErrorString(_e);       \
+            return _e == cudaErrorMemoryAllocation ? ERP_ENOMEM : ERP_ECUDA;  \
+        }                                                                      \
+    } while (0)
+
+static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c) {
+    erp_params prm;
+    memset(&prm, 0, sizeof prm);
+    if (pp) prm = *pp;
+    if (prm.num_bins_x == 0) prm.num_bins_x = 512;
+    if (prm.num_bins_y == 0) prm.num_bins_y = 512;
+    if (!pow2_ok(prm.num_bins_x) || !pow2_ok(prm.num_bins_y)) {
+        c.err = "bin counts must be powers of two in [16, 4096]";
+        return ERP_EINVAL;
+    }
+    if (prm.precision != ERP_PREC_FP32) {
+        c.err = "unsupported precision";
+        return ERP_ENOTSUP;
+    }
+    erp_status s = validate(d, c.err);
+    if (s != ERP_OK) return s;
+    s = check_device(prm.device, c.err);
+    if (s != ERP_OK) return s;
+    c.device = prm.device;
+    CK(spectral_prepare());
+    const int N = d->num_nodes, NM = d->num_movable, P = d->num_pins, E = d->num_nets;
+    c.N = N; c.NM = NM; c.P = P; c.E = E; c.NS = P;
+    c.m = prm.num_bins_x; c.n = prm.num_bins_y;
+    c.logm = ilog2(c.m); c.logn = ilog2(c.n);
+    c.die_w = d->die_w; c.die_h = d->die_h;
+    // Bins::new (src/placement.rs:49-66)
+    c.bin_w = d->die_w / (float)c.m;
+    c.bin_h = d->die_h / (float)c.n;
+    c.inv_bw = 1.0f / c.bin_w;
+    c.inv_bh = 1.0f / c.bin_h;
+    c.bin_area = c.bin_w * c.bin_h;
+    c.inv_bin_area = 1.0f / c.bin_area;
+    c.target_density = prm.target_density >= 0 ? prm.target_density : d->cell_utilization;
+    c.movable_area = d->movable_area;
+    if (!(c.movable_area > 0)) {
+        c.err = "movable_area must be positive";
+        return ERP_EINVAL;
+    }
+    if (prm.stream) {
+        c.stream = (cudaStream_t)prm.stream;
+        c.own_stream = false;
+    } else {
+        CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        c.own_stream = true;
+    }
+    // --- cells: PlacementSolution::new + PotentialComputation::new sizes ---
+    std::vector<float> hx(N), hy(N), hcw(N), hch(N), hox(N), hoy(N), hr(N);
+    const float cxm = d->die_w / 2.0f, cym = d->die_h / 2.0f;
+    const float sqrt2 = 1.41421356237309504880f;
+    double mov_tot = 0, fix_tot = 0;
+    for (int i = 0; i < N; ++i) {
+        const float w = d->w[i], h = d->h[i];
+        if (i >= NM || prm.start_mode == ERP_START_DB) {
+            hx[i] = d->x[i]; hy[i] = d->y[i];
+        } else {
+            hx[i] = cxm - w / 2.0f;                       // src/placement.rs:129-130
+            hy[i] = cym - h / 2.0f;
+        }
+        const float cw = fmaxf(w, c.bin_w * sqrt2), ch = fmaxf(h, c.bin_h * sqrt2);   // src/epotential.rs:88-92
+        float r = (w * h) / (cw * ch);
+        if (i >= NM) r = c.target_density;
+        hcw[i] = cw; hch[i] = ch;
+        hox[i] = (w - cw) * 0.5f; hoy[i] = (h - ch) * 0.5f;
+        hr[i] = r;
+        if (i < NM) mov_tot += (double)w * (double)h;
+        else fix_tot += (double)w * (double)h;
+    }
+    c.shift = fixed_shift(mov_tot);
+    c.shift0 = fixed_shift(fix_tot);
+    c.fixed_scale = ldexpf(1.0f, c.shift);
+    c.fixed_inv = ldexpf(1.0f, -c.shift);
+    // --- nets: degree classes, internal order, pin slots ---
+    std::vector<int> cls_of(E);
+    int counts[kNumClasses] = {0};
+    for (int e = 0; e < E; ++e) {
+        const int deg = d->net_ptr[e + 1] - d->net_ptr[e];
+        int k;
+        if (e < d->n_2nets) k = 0;
+        else if (deg <= 4) k = 1;
+        else if (deg <= 8) k = 2;
+        else if (deg <= 16) k = 3;
+        else if (deg <= 32) k = 4;
+        else k = 5;
+        cls_of[e] = k;
+        counts[k]++;
+    }
+    const int widths[kNumClasses] = {2, 4, 8, 16, 32, 32};
+    int begin = 0;
+    for (int k = 0; k < kNumClasses; ++k) {
+        c.cls[k].begin = begin;
+        c.cls[k].count = counts[k];
+        c.cls[k].width = widths[k];
+        c.cls[k].general = k == 0 ? 0 : 1;
+        begin += counts[k];
+    }
+    std::vector<int> fill(kNumClasses);
+    for (int k = 0; k < kNumClasses; ++k) fill[k] = c.cls[k].begin;
+    c.h_net_of_internal = new int32_t[E > 0 ? E : 1];
+    for (int e = 0; e < E; ++e) c.h_net_of_internal[fill[cls_of[e]]++] = e;
+    std::vector<int32_t> hnet_ptr(E + 1, 0), hslot_cell(P), hcell_ptr(NM + 1, 0);
+    std::vector<float2> hslot_off(P);
+    c.h_slot_of_pin = new int32_t[P > 0 ? P : 1];
+    for (int p = 0; p < P; ++p) c.h_slot_of_pin[p] = -1;
+    int slot = 0;
+    for (int ie = 0; ie < E; ++ie) {
+        const int e = c.h_net_of_internal[ie];
+        hnet_ptr[ie] = slot;
+        for (int k = d->net_ptr[e]; k < d->net_ptr[e + 1]; ++k) c.h_slot_of_pin[d->net_pins[k]] = slot++;
+    }
+    hnet_ptr[E] = slot;
+    for (int p = 0; p < P; ++p)
+        if (c.h_slot_of_pin[p] < 0) c.h_slot_of_pin[p] = slot++;   // unconnected pins: gradient stays 0
+    for (int p = 0; p < P; ++p) {
+        const int sl = c.h_slot_of_pin[p];
+        hslot_cell[sl] = d->pin_inst[p];
+        hslot_off[sl] = make_float2(d->pin_ox[p], d->pin_oy[p]);
+    }
+    for (int i = 0; i < NM; ++i) hcell_ptr[i + 1] = hcell_ptr[i] + (d->inst_pin_ptr[i + 1] - d->inst_pin_ptr[i]);
+    std::vector<int32_t> hcell_slots(hcell_ptr[NM]);
+    for (int i = 0; i < NM; ++i)
+        for (int k = d->inst_pin_ptr[i], o = hcell_ptr[i]; k < d->inst_pin_ptr[i + 1]; ++k, ++o)
+            hcell_slots[o] = c.h_slot_of_pin[d->inst_pins[k]];
+    // --- device allocations ---
+    const size_t mn = (size_t)c.m * c.n;
+    float **cellarr[] = {&c.x, &c.y, &c.w, &c.h, &c.npins, &c.cw, &c.ch, &c.offx, &c.offy, &c.ratio,
+                         &c.wlgx, &c.wlgy, &c.dgx, &c.dgy, &c.prev_x, &c.prev_y, &c.prev_gx, &c.prev_gy};
+    for (float **a : cellarr) CK(dalloc(a, (size_t)N + 4));
+    CK(dalloc(&c.slot_cell, P));
+    CK(dalloc(&c.slot_off, P));
+    CK(dalloc(&c.slot_grad, P));
+    CK(dalloc(&c.net_ptr, (size_t)E + 1));
+    CK(dalloc(&c.net_hpwl, E));
+    CK(dalloc(&c.cell_slot_ptr, (size_t)NM + 1));
+    CK(dalloc(&c.cell_slots, hcell_slots.size()));
+    CK(dalloc(&c.dmap, mn));
+    float **maps[] = {&c.initial, &c.rho, &c.t1, &c.tx, &c.ty, &c.tp, &c.fx, &c.fy, &c.psi};
+    for (float **a : maps) CK(dalloc(a, mn));
+    CK(dalloc(&c.partials, kMaxPartials));
+    c.max_partials = kMaxPartials;
+    CK(dalloc(&c.st, 1));
+    CK(cudaMallocHost((void **)&c.h_st, sizeof(DevState)));
+    spectral_tables(c.m, c.n, c.bin_w, c.bin_h, &c.tw_m, &c.tw_n, &c.ek_m, &c.ek_n, &c.wu, &c.wv, c.stream);
+    CK(cudaGetLastError());
+    // --- uploads ---
+    CK(upload(c.x, hx.data(), sizeof(float) * N, c.stream));
+    CK(upload(c.y, hy.data(), sizeof(float) * N, c.stream));
+    CK(upload(c.w, d->w, sizeof(float) * N, c.stream));
+    CK(upload(c.h, d->h, sizeof(float) * N, c.stream));
+    CK(upload(c.npins, d->num_pins_f, sizeof(float) * N, c.stream));
+    CK(upload(c.cw, hcw.data(), sizeof(float) * N, c.stream));
+    CK(upload(c.ch, hch.data(), sizeof(float) * N, c.stream));
+    CK(upload(c.offx, hox.data(), sizeof(float) * N, c.stream));
+    CK(upload(c.offy, hoy.data(), sizeof(float) * N, c.stream));
+    CK(upload(c.ratio, hr.data(), sizeof(float) * N, c.stream));
+    // Nesterov::new: prev coords = DB coordinates, prev grads = 0 (src/nesterov.rs:15-24)
+    CK(upload(c.prev_x, d->x, sizeof(float) * N, c.stream));
+    CK(upload(c.prev_y, d->y, sizeof(float) * N, c.stream));
+    for (float *a : {c.prev_gx, c.prev_gy, c.wlgx, c.wlgy, c.dgx, c.dgy})
+        CK(cudaMemsetAsync(a, 0, sizeof(float) * ((size_t)N + 4), c.stream));
+    CK(upload(c.slot_cell, hslot_cell.data(), sizeof(int32_t) * P, c.stream));
+    CK(upload(c.slot_off, hslot_off.data(), sizeof(float2) * P, c.stream));
+    CK(cudaMemsetAsync(c.slot_grad, 0, sizeof(float2) * (P ? P : 1), c.stream));
+    CK(upload(c.net_ptr, hnet_ptr.data(), sizeof(int32_t) * (E + 1), c.stream));
+    CK(upload(c.cell_slot_ptr, hcell_ptr.data(), sizeof(int32_t) * (NM + 1), c.stream));
+    CK(upload(c.cell_slots, hcell_slots.data(), sizeof(int32_t) * hcell_slots.size(), c.stream));
+    CK(cudaMemsetAsync(c.dmap, 0, sizeof(unsigned long long) * mn, c.stream));
+    for (float **a : maps) CK(cudaMemsetAsync(*a, 0, sizeof(float) * mn, c.stream));
+    // scheduler / optimiser state (src/scheduler.rs:52-66, src/nesterov.rs:15-24)
+    DevState h;
+    memset(&h, 0, sizeof h);
+    h.gamma = 4.0f * (c.bin_w + c.bin_h);
+    h.base_gamma = h.gamma;
+    h.dw = 8e-5f;
+    h.alpha = 1.0f;
+    h.beta = 0.0f;
+    *c.h_st = h;
+    CK(cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream));
+    // fixed-cell initial density (src/epotential.rs:127-140)
+    launch_initial_density(c, nullptr, nullptr, nullptr, nullptr);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c.stream));
+    c.map_dirty = false;
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_create(const erp_design *design, const erp_params *params, erp_ctx **out) {
+    g_create_err.clear();
+    if (!out) {
+        g_create_err = "out is NULL";
+        return ERP_EINVAL;
+    }
+    *out = nullptr;
+    erp_ctx *ctx = new (std::nothrow) erp_ctx();  // value-initialised: all pointers null
+    if (!ctx) return ERP_ENOMEM;
+    erp_status s = create_impl(design, params, ctx->c);
+    if (s != ERP_OK) {
+        g_create_err = ctx->c.err;
+        free_ctx(ctx->c);
+        delete ctx;
+        return s;
+    }
+    *out = ctx;
+    return ERP_OK;
+}
+
+extern "C" void erp_destroy(erp_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->c.device);
+    if (ctx->c.stream) cudaStreamSynchronize(ctx->c.stream);
+    free_ctx(ctx->c);
+    delete ctx;
+}
+
+// ---------------------------------------------------------------------------
+#define CTX_CHECK()                        \
+    if (!ctx) return ERP_EINVAL;           \
+    Ctx &c = ctx->c;                       \
+    c.err.clear();                         \
+    if (cudaSetDevice(c.device) != cudaSuccess) { c.err = "cudaSetDevice failed"; return ERP_ECUDA; }
+
+static erp_status pull_state(Ctx &c) {
+    CK(cudaMemcpyAsync(c.h_st, c.st, sizeof(DevState), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    if (c.h_st->status & 1) {
+        c.err = "non-finite HPWL, overflow or step length";
+        return ERP_ENAN;
+    }
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_wirelength(erp_ctx *ctx, float gamma, float *hpwl) {
+    CTX_CHECK();
+    if (!(gamma > 0)) { c.err = "gamma must be positive"; return ERP_EINVAL; }
+    launch_wirelength(c, gamma);
+    launch_wl_gather(c);
+    CK(cudaGetLastError());
+    if (hpwl) {
+        erp_status s = pull_state(c);
+        *hpwl = c.h_st->hpwl_f;
+        return s;
+    }
+    return ERP_OK;
+}
+
+static void enqueue_potential(Ctx &c, bool stage, bool want_psi) {
+    if (stage || c.map_dirty) cudaMemsetAsync(c.dmap, 0, sizeof(unsigned long long) * (size_t)c.m * c.n, c.stream);
+    launch_density_scatter(c);
+    launch_spectral(c, /*zero_map=*/!stage, /*store_rho=*/stage, want_psi);
+    launch_force(c);
+    c.map_dirty = stage;
+}
+
+extern "C" erp_status erp_potential(erp_ctx *ctx, int32_t iteration, float *energy, float *overflow) {
+    CTX_CHECK();
+    (void)iteration;  // selects the reference's density variant; one fixed-point rule here
+    enqueue_potential(c, true, energy != nullptr);
+    if (energy) {
+        launch_energy(c);
+        c.psi_valid = true;
+    }
+    CK(cudaGetLastError());
+    if (energy || overflow) {
+        erp_status s = pull_state(c);
+        if (energy) *energy = (float)c.h_st->energy;
+        if (overflow) *overflow = c.h_st->overflow_f;
+        return s;
+    }
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_nesterov(erp_ctx *ctx, int32_t iteration) {
+    CTX_CHECK();
+    if (iteration < 0) { c.err = "iteration must be >= 0"; return ERP_EINVAL; }
+    launch_nesterov(c, iteration);
+    CK(cudaGetLastError());
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_scheduler_update(erp_ctx *ctx, float hpwl, float overflow) {
+    CTX_CHECK();
+    launch_scheduler(c, 1, hpwl, overflow);
+    CK(cudaGetLastError());
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_should_stop(erp_ctx *ctx, int32_t *stop) {
+    CTX_CHECK();
+    if (!stop) return ERP_EINVAL;
+    erp_status s = pull_state(c);
+    const float cur = c.h_st->hpwl_cur, prev = c.h_st->hpwl_prev;
+    *stop = (prev != 0.0f && cur != 0.0f && prev > cur * 1.5f) ? 1 : 0;   // src/scheduler.rs:75-81
+    return s;
+}
+
+static erp_status ensure_graph(Ctx &c) {
+    if (c.graph_ready) return ERP_OK;
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+    // Placement::step order (src/placement.rs:180-228)
+    launch_wirelength(c, -1.0f);
+    launch_wl_gather(c);
+    launch_density_scatter(c);
+    launch_spectral(c, /*zero_map=*/true, /*store_rho=*/false, /*want_psi=*/false);
+    launch_force(c);
+    launch_nesterov(c, -1);
+    launch_scheduler(c, 0, 0.f, 0.f);
+    cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+    if (e != cudaSuccess) {
+        c.err = std::string("graph capture: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        return ERP_ECUDA;
+    }
+    size_t nn = 0;
+    cudaGraphGetNodes(g, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+    c.graph_kernels = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) c.graph_kernels++;
+    }
+    e = cudaGraphInstantiate(&c.graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        c.err = std::string("graph instantiate: ") + cudaGetErrorString(e);
+        return ERP_ECUDA;
+    }
+    c.graph_ready = true;
+    return ERP_OK;
+}
+
+static erp_status enqueue_step(Ctx &c) {
+    erp_status s = ensure_graph(c);
+    if (s != ERP_OK) return s;
+    if (c.map_dirty) {
+        CK(cudaMemsetAsync(c.dmap, 0, sizeof(unsigned long long) * (size_t)c.m * c.n, c.stream));
+        c.map_dirty = false;
+    }
+    CK(cudaGraphLaunch(c.graph, c.stream));
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_step(erp_ctx *ctx, erp_step_stats *stats) {
+    CTX_CHECK();
+    erp_status s = enqueue_step(c);
+    if (s != ERP_OK) return s;
+    if (stats) {
+        s = pull_state(c);
+        *stats = c.h_st->last;
+        return s;
+    }
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_step_host(erp_ctx *ctx, float *x, float *y, erp_step_stats *stats) {
+    CTX_CHECK();
+    if (!x || !y) return ERP_EINVAL;
+    CK(cudaMemcpyAsync(c.x, x, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.y, y, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+    erp_status s = enqueue_step(c);
+    if (s != ERP_OK) return s;
+    CK(cudaMemcpyAsync(x, c.x, sizeof(float) * c.N, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaMemcpyAsync(y, c.y, sizeof(float) * c.N, cudaMemcpyDeviceToHost, c.stream));
+    s = pull_state(c);
+    if (stats) *stats = c.h_st->last;
+    return s;
+}
+
+extern "C" erp_status erp_run(erp_ctx *ctx, int32_t max_iterations, float stop_overflow,
+                              int32_t *iterations_run, erp_step_stats *last) {
+    CTX_CHECK();
+    if (max_iterations < 0) return ERP_EINVAL;
+    erp_status s = pull_state(c);
+    if (s != ERP_OK) return s;
+    const int start = c.h_st->iteration;
+    // arm the retire flag
+    const float so = stop_overflow > 0 ? stop_overflow : 0.0f;
+    CK(cudaMemcpyAsync(&c.st->stop_overflow, &so, sizeof(float), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemsetAsync(&c.st->done, 0, sizeof(int32_t), c.stream));
+    const int chunk = 16;
+    int launched = 0;
+    cudaEvent_t ev[2];
+    CK(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+    int32_t *h_done = nullptr;
+    CK(cudaMallocHost((void **)&h_done, 2 * sizeof(int32_t)));
+    h_done[0] = h_done[1] = 0;
+    int pending = -1;  // buffer index with an outstanding check
+    bool stop = false;
+    while (!stop && launched < max_iterations) {
+        const int k = std::min(chunk, max_iterations - launched);
+        for (int i = 0; i < k && s == ERP_OK; ++i) s = enqueue_step(c);
+        if (s != ERP_OK) break;
+        launched += k;
+        const int b = (launched / chunk) & 1;
+        CK(cudaMemcpyAsync(&h_done[b], &c.st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaEventRecord(ev[b], c.stream));
+        if (pending >= 0) {
+            CK(cudaEventSynchronize(ev[pending]));
+            if (h_done[pending]) stop = true;
+        }
+        pending = b;
+    }
+    CK(cudaStreamSynchronize(c.stream));
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    cudaFreeHost(h_done);
+    const float zero = 0.0f;
+    CK(cudaMemcpyAsync(&c.st->stop_overflow, &zero, sizeof(float), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemsetAsync(&c.st->done, 0, sizeof(int32_t), c.stream));
+    erp_status s2 = pull_state(c);
+    if (iterations_run) *iterations_run = c.h_st->iteration - start;
+    if (last) *last = c.h_st->last;
+    return s != ERP_OK ? s : s2;
+}
+
+extern "C" erp_status erp_get_scalars(erp_ctx *ctx, erp_scalars *o) {
+    CTX_CHECK();
+    if (!o) return ERP_EINVAL;
+    erp_status s = pull_state(c);
+    const DevState &h = *c.h_st;
+    memset(o, 0, sizeof *o);
+    o->iteration = h.iteration;
+    o->gamma = h.gamma; o->base_gamma = h.base_gamma; o->density_weight = h.dw;
+    o->alpha = h.alpha; o->beta = h.beta;
+    o->hpwl_initial = h.hpwl_init; o->hpwl_current = h.hpwl_cur; o->hpwl_previous = h.hpwl_prev;
+    o->overflow_current = h.ovf_cur; o->overflow_previous = h.ovf_prev;
+    o->hpwl_last = h.hpwl; o->overflow_last = h.overflow; o->energy_last = h.energy;
+    o->fixed_shift = c.shift; o->fixed_shift_init = c.shift0;
+    o->num_bins_x = c.m; o->num_bins_y = c.n;
+    o->bin_w = c.bin_w; o->bin_h = c.bin_h; o->target_density = c.target_density;
+    o->graph_kernels = c.graph_kernels;
+    return s;
+}
+
+extern "C" erp_status erp_set_scalars(erp_ctx *ctx, int32_t iteration, float gamma, float dw,
+                                      float alpha, float beta) {
+    CTX_CHECK();
+    erp_status s = pull_state(c);
+    if (s != ERP_OK) return s;
+    c.h_st->iteration = iteration;
+    c.h_st->gamma = gamma;
+    c.h_st->dw = dw;
+    c.h_st->alpha = alpha;
+    c.h_st->beta = beta;
+    CK(cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_get_positions(erp_ctx *ctx, float *x, float *y) {
+    CTX_CHECK();
+    if (!x || !y) return ERP_EINVAL;
+    CK(cudaMemcpyAsync(x, c.x, sizeof(float) * c.N, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaMemcpyAsync(y, c.y, sizeof(float) * c.N, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_set_positions(erp_ctx *ctx, const float *x, const float *y) {
+    CTX_CHECK();
+    if (!x || !y) return ERP_EINVAL;
+    CK(cudaMemcpyAsync(c.x, x, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.y, y, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_set_nesterov_history(erp_ctx *ctx, const float *px, const float *py,
+                                               const float *pgx, const float *pgy) {
+    CTX_CHECK();
+    if (!px || !py || !pgx || !pgy) return ERP_EINVAL;
+    CK(cudaMemcpyAsync(c.prev_x, px, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.prev_y, py, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.prev_gx, pgx, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.prev_gy, pgy, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_get_array(erp_ctx *ctx, erp_array which, void *dst, size_t bytes) {
+    CTX_CHECK();
+    if (!dst) return ERP_EINVAL;
+    const size_t mn = (size_t)c.m * c.n;
+    const void *src = nullptr;
+    size_t need = 0;
+    switch (which) {
+    case ERP_ARR_WL_GRAD_X: src = c.wlgx; need = sizeof(float) * c.N; break;
+    case ERP_ARR_WL_GRAD_Y: src = c.wlgy; need = sizeof(float) * c.N; break;
+    case ERP_ARR_DENS_GRAD_X: src = c.dgx; need = sizeof(float) * c.N; break;
+    case ERP_ARR_DENS_GRAD_Y: src = c.dgy; need = sizeof(float) * c.N; break;
+    case ERP_ARR_DENSITY_I64: src = c.dmap; need = sizeof(int64_t) * mn; break;
+    case ERP_ARR_DENSITY: src = c.rho; need = sizeof(float) * mn; break;
+    case ERP_ARR_INITIAL: src = c.initial; need = sizeof(float) * mn; break;
+    case ERP_ARR_FIELD_X: src = c.fx; need = sizeof(float) * mn; break;
+    case ERP_ARR_FIELD_Y: src = c.fy; need = sizeof(float) * mn; break;
+    case ERP_ARR_POTENTIAL: src = c.psi; need = sizeof(float) * mn; break;
+    case ERP_ARR_PREV_X: src = c.prev_x; need = sizeof(float) * c.N; break;
+    case ERP_ARR_PREV_Y: src = c.prev_y; need = sizeof(float) * c.N; break;
+    case ERP_ARR_PREV_GX: src = c.prev_gx; need = sizeof(float) * c.N; break;
+    case ERP_ARR_PREV_GY: src = c.prev_gy; need = sizeof(float) * c.N; break;
+    case ERP_ARR_PIN_GRAD_X:
+    case ERP_ARR_PIN_GRAD_Y: {
+        need = sizeof(float) * c.P;
+        if (bytes < need) { c.err = "destination too small"; return ERP_EINVAL; }
+        std::vector<float2> tmp(c.P ? c.P : 1);
+        CK(cudaMemcpyAsync(tmp.data(), c.slot_grad, sizeof(float2) * c.P, cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+        float *o = (float *)dst;
+        for (int p = 0; p < c.P; ++p) {
+            const float2 v = tmp[c.h_slot_of_pin[p]];
+            o[p] = which == ERP_ARR_PIN_GRAD_X ? v.x : v.y;
+        }
+        return ERP_OK;
+    }
+    case ERP_ARR_NET_HPWL: {
+        need = sizeof(float) * c.E;
+        if (bytes < need) { c.err = "destination too small"; return ERP_EINVAL; }
+        std::vector<float> tmp(c.E ? c.E : 1);
+        CK(cudaMemcpyAsync(tmp.data(), c.net_hpwl, sizeof(float) * c.E, cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+        float *o = (float *)dst;
+        for (int ie = 0; ie < c.E; ++ie) o[c.h_net_of_internal[ie]] = tmp[ie];
+        return ERP_OK;
+    }
+    default: c.err = "unknown array"; return ERP_EINVAL;
+    }
+    if (bytes < need) { c.err = "destination too small"; return ERP_EINVAL; }
+    CK(cudaMemcpyAsync(dst, src, need, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_synchronize(erp_ctx *ctx) {
+    CTX_CHECK();
+    CK(cudaStreamSynchronize(c.stream));
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_profile_stages(erp_ctx *ctx, int32_t reps, float *ms_out) {
+    CTX_CHECK();
+    if (reps < 1 || !ms_out) return ERP_EINVAL;
+    const size_t flush_bytes = 256u << 20;
+    void *flush = nullptr;
+    CK(cudaMalloc(&flush, flush_bytes));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const size_t mn = (size_t)c.m * c.n;
+    erp_status rc = ERP_OK;
+    for (int stage = 0; stage < ERP_NUM_STAGES && rc == ERP_OK; ++stage) {
+        double total = 0;
+        for (int r = 0; r <= reps; ++r) {   // r == 0: untimed warm-up
+            cudaMemsetAsync(flush, r & 0xff, flush_bytes, c.stream);
+            cudaEventRecord(e0, c.stream);
+            switch (stage) {
+            case ERP_STAGE_WIRELENGTH: launch_wirelength(c, -1.0f); launch_wl_gather(c); break;
+            case ERP_STAGE_DENSITY:
+                cudaMemsetAsync(c.dmap, 0, sizeof(unsigned long long) * mn, c.stream);
+                launch_density_scatter(c);
+                break;
+            case ERP_STAGE_SPECTRAL: launch_spectral(c, true, false, false); break;
+            case ERP_STAGE_FORCE: launch_force(c); break;
+            case ERP_STAGE_NESTEROV: launch_nesterov(c, -1); break;
+            default: launch_scheduler(c, 0, 0.f, 0.f); break;
+            }
+            cudaEventRecord(e1, c.stream);
+            cudaError_t err = cudaEventSynchronize(e1);
+            if (err != cudaSuccess) {
+                c.err = cudaGetErrorString(err);
+                rc = ERP_ECUDA;
+                break;
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (r > 0) total += ms;
+        }
+        ms_out[stage] = (float)(total / reps);
+    }
+    c.map_dirty = true;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(flush);
+    if (rc == ERP_OK) {
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) { c.err = cudaGetErrorString(err); rc = ERP_ECUDA; }
+    }
+    return rc;
+}
+
+// ---------------------------------------------------------------------------
+// standalone spectral solve
+extern "C" erp_status erp_spectral_create(int32_t m, int32_t n, float bin_w, float bin_h,
+                                          int32_t precision, void *stream, erp_spectral **out) {
+    g_create_err.clear();
+    if (!out || !pow2_ok(m) || !pow2_ok(n) || !(bin_w > 0) || !(bin_h > 0)) {
+        g_create_err = "invalid spectral solve parameters";
+        return ERP_EINVAL;
+    }
+    if (precision != ERP_PREC_FP32) {
+        g_create_err = "unsupported precision";
+        return ERP_ENOTSUP;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    erp_status s = check_device(dev, g_create_err);
+    if (s != ERP_OK) return s;
+    if (spectral_prepare() != cudaSuccess) { g_create_err = "cudaFuncSetAttribute failed"; return ERP_ECUDA; }
+    erp_spectral *sp = new erp_spectral();
+    SpectralPlan &p = sp->p;
+    memset(&p, 0, sizeof p);
+    p.m = m; p.n = n; p.logm = ilog2(m); p.logn = ilog2(n);
+    p.bin_w = bin_w; p.bin_h = bin_h;
+    p.stream = (cudaStream_t)stream;
+    const size_t mn = (size_t)m * n;
+    bool ok = cudaMalloc(&p.t1, sizeof(float) * mn) == cudaSuccess &&
+              cudaMalloc(&p.tx, sizeof(float) * mn) == cudaSuccess &&
+              cudaMalloc(&p.ty, sizeof(float) * mn) == cudaSuccess &&
+              cudaMalloc(&p.tp, sizeof(float) * mn) == cudaSuccess &&
+              cudaMalloc(&sp->st, sizeof(DevState)) == cudaSuccess;
+    if (!ok) {
+        cudaFree(p.t1); cudaFree(p.tx); cudaFree(p.ty); cudaFree(p.tp); cudaFree(sp->st);
+        delete sp;
+        g_create_err = "device allocation failed";
+        return ERP_ENOMEM;
+    }
+    cudaMemsetAsync(sp->st, 0, sizeof(DevState), p.stream);
+    spectral_tables(m, n, bin_w, bin_h, &p.tw_m, &p.tw_n, &p.ek_m, &p.ek_n, &p.wu, &p.wv, p.stream);
+    p.st = sp->st;
+    if (cudaGetLastError() != cudaSuccess) {
+        g_create_err = "spectral table set-up failed";
+        erp_spectral_destroy(sp);
+        return ERP_ECUDA;
+    }
+    *out = sp;
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_spectral_solve(erp_spectral *sp, const float *rho, float *fx, float *fy,
+                                         float *psi) {
+    if (!sp || !rho || !fx || !fy) return ERP_EINVAL;
+    SpectralArgs a;
+    a.rho_in = rho;
+    a.fx = fx;
+    a.fy = fy;
+    a.psi = psi;
+    a.st = sp->st;
+    launch_spectral_plan(sp->p, a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        sp->err = cudaGetErrorString(e);
+        return ERP_ECUDA;
+    }
+    return ERP_OK;
+}
+
+extern "C" void erp_spectral_destroy(erp_spectral *sp) {
+    if (!sp) return;
+    SpectralPlan &p = sp->p;
+    void *ptrs[] = {p.t1, p.tx, p.ty, p.tp, p.tw_m, p.tw_n, p.ek_m, p.ek_n, p.wu, p.wv, sp->st};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    delete sp;
+}

@@ -1,0 +1,163 @@
+// Internal definitions shared by the CUDA translation units of
+// liberplacer_gb300.so: the device-resident context layout, the scalar state
+// the whole iteration keeps on the device, and the kernel launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "erplacer.h"
+
+namespace erp {
+
+constexpr int kThreads = 256;
+
+// Device-resident scalars.  Every quantity the reference keeps in Scheduler /
+// Nesterov (src/scheduler.rs:37-50, src/nesterov.rs:6-13) plus the reductions
+// of the current step, so that a whole Placement::step runs without a host
+// round trip (FP64 for the HPWL / overflow totals, the Lipschitz sums and the
+// density-weight update).
+struct DevState {
+    // scheduler
+    int32_t iteration;
+    int32_t hpwl_init_set;
+    float gamma, base_gamma, dw;
+    float hpwl_init, hpwl_cur, hpwl_prev;
+    float ovf_init, ovf_cur, ovf_prev;
+    int32_t ovf_init_set;
+    // optimiser
+    float alpha, beta;
+    // this step's reductions
+    double hpwl;
+    double overflow;
+    double energy;
+    double lip_num, lip_den;
+    double abs_wl, abs_dens;
+    float hpwl_f, overflow_f;
+    // step bookkeeping
+    int32_t done;          // set once overflow <= stop threshold: kernels become no-ops
+    int32_t status;        // bit 0: non-finite value seen
+    float stop_overflow;   // <= 0: never stop
+    int32_t last_iter;     // iteration index of the last completed step
+    erp_step_stats last;   // stats of the last completed step
+    // last-block counters of the deterministic reductions
+    uint32_t ctr[8];
+};
+
+enum Counter { CTR_HPWL = 0, CTR_OVF = 1, CTR_ABS = 2, CTR_LIP = 3, CTR_ENERGY = 4 };
+
+// Net degree classes processed by one thread group of width W each.
+constexpr int kNumClasses = 6;  // fast 2-pin, <=4, <=8, <=16, <=32, >32
+struct NetClass {
+    int32_t begin, count;  // range in the internal net order
+    int32_t width;         // lanes per net
+    int32_t general;       // 1: general path (min/max initialised to die+1 / 0)
+};
+
+struct Ctx {
+    // --- sizes ---
+    int32_t N, NM, P, E, NS;   // nodes, movable, pins, nets, pin slots (= P)
+    int32_t m, n, logm, logn;
+    float die_w, die_h, bin_w, bin_h, inv_bw, inv_bh, bin_area, inv_bin_area;
+    float target_density, movable_area;
+    int32_t shift, shift0;
+    float fixed_scale, fixed_inv;
+    int device;
+    cudaStream_t stream;
+    bool own_stream;
+    std::string err;
+    // --- cells [N] ---
+    float *x, *y, *w, *h, *npins, *cw, *ch, *offx, *offy, *ratio;
+    float *wlgx, *wlgy, *dgx, *dgy;
+    float *prev_x, *prev_y, *prev_gx, *prev_gy;
+    // --- pins in internal slot order [NS] ---
+    int32_t *slot_cell;
+    float2 *slot_off;
+    float2 *slot_grad;
+    int32_t *net_ptr;          // [E+1] internal order
+    float *net_hpwl;           // [E] internal order
+    NetClass cls[kNumClasses];
+    int32_t *cell_slot_ptr;    // [NM+1]
+    int32_t *cell_slots;
+    // host-side permutations for test hooks
+    int32_t *h_slot_of_pin;    // [P]
+    int32_t *h_net_of_internal;// [E]
+    // --- maps [m*n] ---
+    unsigned long long *dmap;  // int64 fixed-point movable density
+    float *initial, *rho, *t1, *tx, *ty, *tp, *fx, *fy, *psi;
+    float2 *tw_m, *tw_n, *ek_m, *ek_n;   // FFT twiddles and DCT post-twiddles
+    float *wu, *wv;            // frequency vectors [m], [n]
+    bool map_dirty;
+    bool psi_valid;
+    // --- reductions ---
+    double *partials;          // kMaxPartials
+    int32_t max_partials;
+    DevState *st;
+    DevState *h_st;            // pinned host mirror
+    // --- graph ---
+    cudaGraphExec_t graph;
+    bool graph_ready;
+    int32_t graph_kernels;
+    // --- timing hooks (bench): events around the dominant kernel ---
+};
+
+constexpr int kMaxPartials = 8192;
+
+// ---------------- launchers (stream = ctx.stream) ----------------
+// wirelength (src/hpwl.rs)
+void launch_wirelength(Ctx &c, float gamma_arg);          // gamma_arg < 0: read DevState.gamma
+void launch_wl_gather(Ctx &c);
+// density + spectral + force (src/density.rs, src/epotential.rs, src/eforce.rs)
+void launch_initial_density(Ctx &c, const float *hx, const float *hy, const float *hw,
+                            const float *hh);               // setup, on device
+void launch_density_scatter(Ctx &c);
+void launch_spectral(Ctx &c, bool zero_map, bool store_rho, bool want_psi);
+void launch_force(Ctx &c);
+void launch_energy(Ctx &c);
+// optimiser + scheduler (src/nesterov.rs, src/scheduler.rs)
+void launch_nesterov(Ctx &c, int iter_arg);                // iter_arg < 0: read DevState.iteration
+void launch_scheduler(Ctx &c, int use_args, float hpwl, float overflow);
+
+// spectral engine for the standalone solve
+struct SpectralPlan {
+    int32_t m, n, logm, logn;
+    float bin_w, bin_h;
+    float2 *tw_m, *tw_n, *ek_m, *ek_n;
+    float *wu, *wv;
+    float *t1, *tx, *ty, *tp;
+    double *partials;
+    DevState *st;
+    cudaStream_t stream;
+};
+void spectral_tables(int m, int n, float bin_w, float bin_h, float2 **tw_m, float2 **tw_n,
+                     float2 **ek_m, float2 **ek_n, float **wu, float **wv, cudaStream_t s);
+struct SpectralArgs {
+    const float *rho_in = nullptr;          // standalone: rho given directly
+    unsigned long long *dmap = nullptr;     // loop: int64 fixed-point movable map
+    const float *initial = nullptr;         // loop: fixed-cell map
+    float fixed_inv = 0.f, coef = 0.f, inv_bin_area = 0.f;
+    double movable_area = 1.0;
+    bool zero_map = false;
+    float *rho_out = nullptr;
+    float *fx = nullptr, *fy = nullptr, *psi = nullptr;
+    double *partials = nullptr;
+    DevState *st = nullptr;
+};
+void launch_spectral_plan(const SpectralPlan &p, const SpectralArgs &a);
+cudaError_t spectral_prepare();
+size_t spectral_smem_bytes(int m, int n);
+
+int ilog2(int v);
+
+}  // namespace erp
+
+#define ERP_CUDA_CHECK_RET(c, expr)                                                  \
+    do {                                                                             \
+        cudaError_t _e = (expr);                                                     \
+        if (_e != cudaSuccess) {                                                     \
+            (c).err = std::string(#expr) + ": " + cudaGetErrorString(_e);           \
+            return ERP_ECUDA;                                                        \
+        }                                                                            \
+    } while (0)

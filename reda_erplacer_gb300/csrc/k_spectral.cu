@@ -1,0 +1,392 @@
+// Spectral Poisson solve of compute_potential (src/epotential.rs:284-343) as
+// three shared-memory FFT passes over the bin grid (row index = x bin, m rows;
+// column index = y bin, n columns; src/epotential.rs:237-238):
+//
+//   R1  rows, length n:    t1 = DCT-II_n(rho)                 (rho fused from the
+//                          int64 density map + fixed-cell map, with the overflow sum)
+//   C1  columns, length m: A  = (4/(mn)) DCT-II_m(t1); then per column the
+//                          weighted spectra A*wu/2k^2, A*wv/2k^2 (and A/k^2) go
+//                          through IDXST_m / IDCT_m (/ IDCT_m)       -> tx, ty (tp)
+//   R2  rows, length n:    field_x = IDCT_n(tx), field_y = IDXST_n(ty), psi = IDCT_n(tp)
+//
+// The per-axis transforms are the closed forms of the reference pipelines
+// (dct2_fft2 / idxst_idct / idct_idxst / idct2, src/dct2d.rs, src/idct2.rs,
+// src/idct_idxst.rs, src/idxst_idct.rs, checked separable by impulse probing):
+//   DCT-II  y[k] = sum_i x[i] cos(pi k (2i+1) / 2N)                 (x 2/N per axis)
+//   IDCT    y[i] = sum_u c_u X[u] cos(pi u (2i+1) / 2N),  c = (1, 2, 2, ...)
+//   IDXST   y[i] = sum_u c_u X[u] sin(pi u (2i+1) / 2N) = (-1)^i IDCT(X')[i],
+//           X'[0] = 0, X'[u] = X[N-u]
+// Each is computed with Makhoul's length-N complex FFT; two real rows (or
+// columns) share one complex FFT (real + imaginary part), since the forward
+// input is real and the inverse spectra are Hermitian.  The FFT is an in-place
+// radix-2 decimation-in-frequency pass in shared memory (natural order in,
+// bit-reversed order out), twiddles from FP64-computed tables.
+#include "erp_internal.cuh"
+#include "reduce.cuh"
+
+namespace erp {
+
+__device__ __forceinline__ int brev(int k, int logN) { return (int)(__brev((unsigned)k) >> (32 - logN)); }
+
+// In-place radix-2 DIF over nseq sequences of length N (buf[q*N + i]).
+template <bool INV>
+__device__ __forceinline__ void fft_dif(float2 *buf, int nseq, int N, int logN, const float2 *tw) {
+    const int half = N >> 1;
+    const int nbf = nseq * half;
+    for (int s = 0; s < logN; ++s) {
+        const int lh = logN - 1 - s;
+        const int h = 1 << lh;
+        for (int b = threadIdx.x; b < nbf; b += blockDim.x) {
+            const int q = b >> (logN - 1);
+            const int r = b & (half - 1);
+            const int j = r & (h - 1);
+            const int i0 = (q << logN) + ((r >> lh) << (lh + 1)) + j;
+            const int i1 = i0 + h;
+            const float2 a = buf[i0], c = buf[i1];
+            float2 w = tw[j << s];
+            if (INV) w.y = -w.y;
+            const float dx = a.x - c.x, dy = a.y - c.y;
+            buf[i0] = make_float2(a.x + c.x, a.y + c.y);
+            buf[i1] = make_float2(dx * w.x - dy * w.y, dx * w.y + dy * w.x);
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ int makhoul_pos(int i, int N) { return (i & 1) ? (N - 1 - (i >> 1)) : (i >> 1); }
+
+// IDCT spectrum Vi[u] = e^{i pi u / 2N} (X[u] - i X[N-u]); e = ek[u] = (cos, -sin)
+__device__ __forceinline__ float2 idct_spec(float xu, float xnu, float2 e) {
+    const float c = e.x, s = -e.y;
+    return make_float2(c * xu + s * xnu, s * xu - c * xnu);
+}
+
+// ---------------- R1: rows forward DCT-II ----------------
+// PAIRS row pairs per block.  Input either the density map (int64 fixed point +
+// fixed-cell map, converted exactly as the oracle replays it) or rho directly.
+template <int PAIRS>
+__global__ void __launch_bounds__(kThreads) k_rows_dct(
+    int m, int n, int logn, const float2 *__restrict__ tw_g, const float2 *__restrict__ ek_n,
+    const float *__restrict__ rho_in, unsigned long long *__restrict__ dmap,
+    const float *__restrict__ initial, float fixed_inv, float coef, float inv_area, int zero_map,
+    float *__restrict__ rho_out, float *__restrict__ t1, double *__restrict__ partials,
+    DevState *__restrict__ st, double movable_area) {
+    if (st && st->done) return;
+    extern __shared__ float2 sm[];
+    float2 *tw = sm;
+    float2 *buf = sm + (n >> 1);
+    __shared__ double shr[kThreads / 32];
+    for (int k = threadIdx.x; k < (n >> 1); k += blockDim.x) tw[k] = tw_g[k];
+    const int row0 = blockIdx.x * 2 * PAIRS;
+    double ovf = 0.0;
+    for (int idx = threadIdx.x; idx < PAIRS * n; idx += blockDim.x) {
+        const int p = idx >> logn, i = idx & (n - 1);
+        float v[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int r = row0 + 2 * p + h;
+            const size_t k = (size_t)r * n + i;
+            if (rho_in) {
+                v[h] = rho_in[k];
+            } else {
+                const unsigned long long q = dmap[k];
+                if (zero_map) dmap[k] = 0ull;
+                // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
+                const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q), fixed_inv), initial[k]);
+                const float o = __fsub_rn(d, coef);
+                ovf += (double)(o > 0.0f ? o : 0.0f);      // src/epotential.rs:274-276
+                v[h] = __fmul_rn(d, inv_area);               // src/epotential.rs:284-285
+                if (rho_out) rho_out[k] = v[h];
+            }
+        }
+        buf[(p << logn) + makhoul_pos(i, n)] = make_float2(v[0], v[1]);
+    }
+    __syncthreads();
+    fft_dif<false>(buf, PAIRS, n, logn, tw);
+    for (int idx = threadIdx.x; idx < PAIRS * n; idx += blockDim.x) {
+        const int p = idx >> logn, k = idx & (n - 1);
+        const int kk = (n - k) & (n - 1);
+        const float2 A = buf[(p << logn) + brev(k, logn)];
+        float2 B = buf[(p << logn) + brev(kk, logn)];
+        B.y = -B.y;
+        const float2 e = ek_n[k];
+        const float sx = A.x + B.x, sy = A.y + B.y, dx = A.x - B.x, dy = A.y - B.y;
+        const int r = row0 + 2 * p;
+        t1[(size_t)r * n + k] = 0.5f * (e.x * sx - e.y * sy);
+        t1[(size_t)(r + 1) * n + k] = 0.5f * (e.x * dy + e.y * dx);
+    }
+    if (!rho_in && partials) {
+        const double b = block_sum(ovf, shr);
+        double vals[1] = {b};
+        if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_OVF], gridDim.x)) {
+            const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
+            if (threadIdx.x == 0) {
+                st->overflow = tot;
+                st->overflow_f = (float)(tot / movable_area);
+                st->ctr[CTR_OVF] = 0;
+            }
+        }
+    }
+}
+
+// weights of src/frequencies.rs:4-72 evaluated exactly as the oracle does
+__device__ __forceinline__ float inv_k2(int u, int j, const float *wu, const float *wv) {
+    if (u == 0 && j == 0) return 0.0f;
+    const float s = __fadd_rn(__fmul_rn(wu[u], wu[u]), __fmul_rn(wv[j], wv[j]));
+    return __fdiv_rn(1.0f, s);
+}
+
+// ---------------- C1: columns DCT-II, weights, inverse along m ----------------
+template <int CP>
+__global__ void __launch_bounds__(kThreads) k_cols(
+    int m, int n, int logm, const float2 *__restrict__ tw_g, const float2 *__restrict__ ek_m,
+    const float *__restrict__ wu, const float *__restrict__ wv, const float *__restrict__ t1,
+    float *__restrict__ tx, float *__restrict__ ty, float *__restrict__ tp, float scale4,
+    const DevState *__restrict__ st) {
+    if (st && st->done) return;
+    constexpr int CB = 2 * CP;
+    extern __shared__ float2 sm[];
+    float2 *tw = sm;
+    float2 *buf = sm + (m >> 1);
+    float *A = reinterpret_cast<float *>(buf + CP * m);
+    const int j0 = blockIdx.x * CB;
+    for (int k = threadIdx.x; k < (m >> 1); k += blockDim.x) tw[k] = tw_g[k];
+    float *bf = reinterpret_cast<float *>(buf);
+    for (int idx = threadIdx.x; idx < m * CB; idx += blockDim.x) {
+        const int i = idx / CB, c = idx - i * CB;
+        const float v = t1[(size_t)i * n + j0 + c];
+        bf[2 * (((c >> 1) << logm) + makhoul_pos(i, m)) + (c & 1)] = v;
+    }
+    __syncthreads();
+    fft_dif<false>(buf, CP, m, logm, tw);
+    for (int idx = threadIdx.x; idx < CP * m; idx += blockDim.x) {
+        const int p = idx >> logm, u = idx & (m - 1);
+        const int uu = (m - u) & (m - 1);
+        const float2 Az = buf[(p << logm) + brev(u, logm)];
+        float2 Bz = buf[(p << logm) + brev(uu, logm)];
+        Bz.y = -Bz.y;
+        const float2 e = ek_m[u];
+        const float sx = Az.x + Bz.x, sy = Az.y + Bz.y, dx = Az.x - Bz.x, dy = Az.y - Bz.y;
+        A[(2 * p) * m + u] = scale4 * (0.5f * (e.x * sx - e.y * sy));
+        A[(2 * p + 1) * m + u] = scale4 * (0.5f * (e.x * dy + e.y * dx));
+    }
+    __syncthreads();
+    const int nkinds = tp ? 3 : 2;
+    for (int kind = 0; kind < nkinds; ++kind) {
+        // kind 0: field_x  IDXST_m of A*wu_half; kind 1: field_y IDCT_m of A*wv_half;
+        // kind 2: potential IDCT_m of A*inv
+        const bool sine = kind == 0;
+        for (int idx = threadIdx.x; idx < CP * ((m >> 1) + 1); idx += blockDim.x) {
+            const int p = idx / ((m >> 1) + 1), u = idx - p * ((m >> 1) + 1);
+            const int un = (m - u) & (m - 1);   // partner index (u = 0 pairs with "m", i.e. zero)
+            float2 z_u = make_float2(0.f, 0.f), z_n = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c = 2 * p + h, j = j0 + c;
+                const float a_u = A[c * m + u], a_n = A[c * m + un];
+                float wgt_u, wgt_n;
+                const float iu = inv_k2(u, j, wu, wv), in_ = inv_k2(un, j, wu, wv);
+                if (kind == 0) {
+                    wgt_u = __fmul_rn(__fmul_rn(wu[u], iu), 0.5f);
+                    wgt_n = __fmul_rn(__fmul_rn(wu[un], in_), 0.5f);
+                } else if (kind == 1) {
+                    wgt_u = __fmul_rn(__fmul_rn(wv[j], iu), 0.5f);
+                    wgt_n = __fmul_rn(__fmul_rn(wv[j], in_), 0.5f);
+                } else {
+                    wgt_u = iu;
+                    wgt_n = in_;
+                }
+                const float xu = __fmul_rn(a_u, wgt_u);
+                const float xn = (u == 0) ? 0.0f : __fmul_rn(a_n, wgt_n);   // X[m] := 0
+                float2 vu, vn;
+                if (!sine) {
+                    vu = idct_spec(xu, xn, ek_m[u]);
+                    vn = idct_spec(xn, xu, ek_m[un]);
+                } else {
+                    vu = (u == 0) ? make_float2(0.f, 0.f) : idct_spec(xn, xu, ek_m[u]);
+                    vn = idct_spec(xu, xn, ek_m[un]);
+                }
+                if (h == 0) {
+                    z_u.x += vu.x; z_u.y += vu.y; z_n.x += vn.x; z_n.y += vn.y;
+                } else {  // + i * V_b
+                    z_u.x -= vu.y; z_u.y += vu.x; z_n.x -= vn.y; z_n.y += vn.x;
+                }
+            }
+            buf[(p << logm) + u] = z_u;
+            if (u != 0 && u != (m >> 1)) buf[(p << logm) + un] = z_n;
+        }
+        __syncthreads();
+        fft_dif<true>(buf, CP, m, logm, tw);
+        float *out = kind == 0 ? tx : (kind == 1 ? ty : tp);
+        for (int idx = threadIdx.x; idx < m * CB; idx += blockDim.x) {
+            const int i = idx / CB, c = idx - i * CB;
+            const int t = i >> 1, src = (i & 1) ? (m - 1 - t) : t;
+            const float2 w = buf[((c >> 1) << logm) + brev(src, logm)];
+            float v = (c & 1) ? w.y : w.x;
+            if (sine && (i & 1)) v = -v;
+            out[(size_t)i * n + j0 + c] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------- R2: rows inverse along n ----------------
+template <int PAIRS>
+__global__ void __launch_bounds__(kThreads) k_rows_inv(
+    int m, int n, int logn, const float2 *__restrict__ tw_g, const float2 *__restrict__ ek_n,
+    const float *__restrict__ tx, const float *__restrict__ ty, const float *__restrict__ tp,
+    float *__restrict__ fx, float *__restrict__ fy, float *__restrict__ psi,
+    const DevState *__restrict__ st) {
+    if (st && st->done) return;
+    extern __shared__ float2 sm[];
+    float2 *tw = sm;
+    float2 *buf = sm + (n >> 1);
+    for (int k = threadIdx.x; k < (n >> 1); k += blockDim.x) tw[k] = tw_g[k];
+    const int row0 = blockIdx.x * 2 * PAIRS;
+    const int nkinds = tp ? 3 : 2;
+    for (int kind = 0; kind < nkinds; ++kind) {
+        // kind 0: field_x = IDCT_n(tx); kind 1: field_y = IDXST_n(ty); kind 2: psi = IDCT_n(tp)
+        const float *in = kind == 0 ? tx : (kind == 1 ? ty : tp);
+        float *out = kind == 0 ? fx : (kind == 1 ? fy : psi);
+        const bool sine = kind == 1;
+        for (int idx = threadIdx.x; idx < PAIRS * n; idx += blockDim.x) {
+            const int p = idx >> logn, i = idx & (n - 1);
+            const int r = row0 + 2 * p;
+            buf[idx] = make_float2(in[(size_t)r * n + i], in[(size_t)(r + 1) * n + i]);
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < PAIRS * ((n >> 1) + 1); idx += blockDim.x) {
+            const int p = idx / ((n >> 1) + 1), u = idx - p * ((n >> 1) + 1);
+            const int un = (n - u) & (n - 1);
+            const float2 xu2 = buf[(p << logn) + u];
+            const float2 xn2 = (u == 0) ? make_float2(0.f, 0.f) : buf[(p << logn) + un];
+            float2 z_u = make_float2(0.f, 0.f), z_n = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const float xu = h ? xu2.y : xu2.x, xn = h ? xn2.y : xn2.x;
+                float2 vu, vn;
+                if (!sine) {
+                    vu = idct_spec(xu, xn, ek_n[u]);
+                    vn = idct_spec(xn, xu, ek_n[un]);
+                } else {
+                    vu = (u == 0) ? make_float2(0.f, 0.f) : idct_spec(xn, xu, ek_n[u]);
+                    vn = idct_spec(xu, xn, ek_n[un]);
+                }
+                if (h == 0) {
+                    z_u.x += vu.x; z_u.y += vu.y; z_n.x += vn.x; z_n.y += vn.y;
+                } else {
+                    z_u.x -= vu.y; z_u.y += vu.x; z_n.x -= vn.y; z_n.y += vn.x;
+                }
+            }
+            buf[(p << logn) + u] = z_u;
+            if (u != 0 && u != (n >> 1)) buf[(p << logn) + un] = z_n;
+        }
+        __syncthreads();
+        fft_dif<true>(buf, PAIRS, n, logn, tw);
+        for (int idx = threadIdx.x; idx < PAIRS * n; idx += blockDim.x) {
+            const int p = idx >> logn, i = idx & (n - 1);
+            const int t = i >> 1, src = (i & 1) ? (n - 1 - t) : t;
+            const float2 w = buf[(p << logn) + brev(src, logn)];
+            float va = w.x, vb = w.y;
+            if (sine && (i & 1)) { va = -va; vb = -vb; }
+            const int r = row0 + 2 * p;
+            out[(size_t)r * n + i] = va;
+            out[(size_t)(r + 1) * n + i] = vb;
+        }
+        __syncthreads();
+    }
+}
+
+int ilog2(int v) {
+    int l = 0;
+    while ((1 << l) < v) ++l;
+    return l;
+}
+
+static size_t rows_smem(int n, int pairs) { return sizeof(float2) * ((size_t)(n >> 1) + (size_t)pairs * n); }
+static size_t cols_smem(int m, int cp) {
+    return sizeof(float2) * ((size_t)(m >> 1) + (size_t)cp * m) + sizeof(float) * (size_t)(2 * cp) * m;
+}
+
+constexpr int kRowPairs = 2;
+
+static int col_pairs(int m) { return m <= 2048 ? 4 : 2; }
+
+void spectral_tables(int m, int n, float bin_w, float bin_h, float2 **tw_m, float2 **tw_n,
+                     float2 **ek_m, float2 **ek_n, float **wu, float **wv, cudaStream_t s) {
+    auto tw = [](int N) {
+        float2 *h = new float2[N / 2];
+        for (int k = 0; k < N / 2; ++k) {
+            double a = -2.0 * 3.14159265358979323846 * (double)k / (double)N;
+            h[k] = make_float2((float)cos(a), (float)sin(a));
+        }
+        return h;
+    };
+    auto ek = [](int N) {
+        float2 *h = new float2[N];
+        for (int k = 0; k < N; ++k) {
+            double a = 3.14159265358979323846 * (double)k / (2.0 * N);
+            h[k] = make_float2((float)cos(a), (float)-sin(a));
+        }
+        return h;
+    };
+    float2 *h_twm = tw(m), *h_twn = tw(n), *h_ekm = ek(m), *h_ekn = ek(n);
+    float *h_wu = new float[m], *h_wv = new float[n];
+    const float tpm = (float)(2.0 * 3.14159265358979323846) / (float)m;
+    for (int i = 0; i < m; ++i) h_wu[i] = (float)i * tpm;
+    const float wv_div = bin_w / bin_h;
+    const float tpn = (float)(2.0 * 3.14159265358979323846) / (float)n;
+    for (int j = 0; j < n; ++j) h_wv[j] = ((float)j * tpn) * wv_div;
+    cudaMalloc(tw_m, sizeof(float2) * (m / 2));
+    cudaMalloc(tw_n, sizeof(float2) * (n / 2));
+    cudaMalloc(ek_m, sizeof(float2) * m);
+    cudaMalloc(ek_n, sizeof(float2) * n);
+    cudaMalloc(wu, sizeof(float) * m);
+    cudaMalloc(wv, sizeof(float) * n);
+    cudaMemcpyAsync(*tw_m, h_twm, sizeof(float2) * (m / 2), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(*tw_n, h_twn, sizeof(float2) * (n / 2), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(*ek_m, h_ekm, sizeof(float2) * m, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(*ek_n, h_ekn, sizeof(float2) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(*wu, h_wu, sizeof(float) * m, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(*wv, h_wv, sizeof(float) * n, cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);
+    delete[] h_twm; delete[] h_twn; delete[] h_ekm; delete[] h_ekn; delete[] h_wu; delete[] h_wv;
+}
+
+// Opt the spectral kernels into large dynamic shared memory on the current device.
+cudaError_t spectral_prepare() {
+    cudaError_t e = cudaFuncSetAttribute(k_rows_dct<kRowPairs>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_inv<kRowPairs>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cols<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cols<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    return e;
+}
+
+size_t spectral_smem_bytes(int m, int n) {
+    size_t a = rows_smem(n, kRowPairs), b = cols_smem(m, col_pairs(m));
+    return a > b ? a : b;
+}
+
+void launch_spectral_plan(const SpectralPlan &p, const SpectralArgs &a) {
+    const int m = p.m, n = p.n;
+    const bool from_map = a.rho_in == nullptr;
+    const int rb = m / (2 * kRowPairs);
+    k_rows_dct<kRowPairs><<<rb, kThreads, rows_smem(n, kRowPairs), p.stream>>>(
+        m, n, p.logn, p.tw_n, p.ek_n, a.rho_in, a.dmap, a.initial, a.fixed_inv, a.coef,
+        a.inv_bin_area, a.zero_map ? 1 : 0, a.rho_out, p.t1, from_map ? a.partials : nullptr, a.st,
+        a.movable_area);
+    const float scale4 = 4.0f / (float)((double)m * (double)n);
+    float *tp = a.psi ? p.tp : nullptr;
+    if (col_pairs(m) == 4)
+        k_cols<4><<<n / 8, kThreads, cols_smem(m, 4), p.stream>>>(m, n, p.logm, p.tw_m, p.ek_m, p.wu,
+                                                                  p.wv, p.t1, p.tx, p.ty, tp, scale4,
+                                                                  a.st);
+    else
+        k_cols<2><<<n / 4, kThreads, cols_smem(m, 2), p.stream>>>(m, n, p.logm, p.tw_m, p.ek_m, p.wu,
+                                                                  p.wv, p.t1, p.tx, p.ty, tp, scale4,
+                                                                  a.st);
+    k_rows_inv<kRowPairs><<<rb, kThreads, rows_smem(n, kRowPairs), p.stream>>>(
+        m, n, p.logn, p.tw_n, p.ek_n, p.tx, p.ty, tp, a.fx, a.fy, a.psi, a.st);
+}
+
+}  // namespace erp

@@ -1,0 +1,184 @@
+"""Host-side mirror of the reference's placement call surface over the C ABI.
+
+    Placement(design, ...)          Placement::new          (src/placement.rs:159-178)
+    .step() -> bool                 Placement::step         (src/placement.rs:180-228)
+    .compute_hpwl(gamma) -> hpwl    compute_hpwl            (src/hpwl.rs:139-343)
+    .compute_potential(it)          compute_potential       (src/epotential.rs:225-374)
+                                    -> (energy, overflow)
+    .step_adaptive(it)              Nesterov::step_adaptive (src/nesterov.rs:27-146)
+    .scheduler_update(h, o)         Scheduler::update       (src/scheduler.rs:68-73)
+    .should_stop() -> bool          Scheduler::should_stop  (src/scheduler.rs:75-81)
+
+Every call runs on the GPU through liberplacer_gb300.so; errors raise ErpError.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import lib as L
+
+
+class Placement:
+    def __init__(self, design, num_bins=(512, 512), target_density=-1.0,
+                 start_mode=L.START_CENTER, device=0, stream=None):
+        self.lib = L.load()
+        self.design = design
+        self._ds = design.to_struct()
+        m, n = num_bins
+        self._params = L.Params(int(m), int(n), float(target_density), int(start_mode),
+                                L.PREC_FP32, int(device), C.c_void_p(stream) if stream else None, 0)
+        h = C.c_void_p()
+        st = self.lib.erp_create(C.byref(self._ds), C.byref(self._params), C.byref(h))
+        L.check(st, None)
+        self.h = h
+        self.N = int(design.num_nodes)
+        self.P = int(design.num_pins)
+        self.E = int(design.num_nets)
+        self.m, self.n = int(m), int(n)
+
+    # -- lifetime --
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.erp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, st):
+        L.check(st, self.h)
+
+    # -- reference stages --
+    def compute_hpwl(self, gamma):
+        out = C.c_float()
+        self._ck(self.lib.erp_wirelength(self.h, float(gamma), C.byref(out)))
+        return float(out.value)
+
+    def compute_potential(self, iteration, want_energy=True):
+        e, o = C.c_float(), C.c_float()
+        self._ck(self.lib.erp_potential(self.h, int(iteration), C.byref(e) if want_energy else None,
+                                        C.byref(o)))
+        return (float(e.value) if want_energy else None), float(o.value)
+
+    def step_adaptive(self, iteration):
+        self._ck(self.lib.erp_nesterov(self.h, int(iteration)))
+
+    def scheduler_update(self, hpwl, overflow):
+        self._ck(self.lib.erp_scheduler_update(self.h, float(hpwl), float(overflow)))
+
+    def should_stop(self):
+        s = C.c_int32()
+        self._ck(self.lib.erp_should_stop(self.h, C.byref(s)))
+        return bool(s.value)
+
+    def step(self, stats=True):
+        """One Placement::step (CUDA-graph replay).  Returns should_stop, or None
+        when stats=False (the call then only enqueues work)."""
+        if not stats:
+            self._ck(self.lib.erp_step(self.h, None))
+            return None
+        st = L.StepStats()
+        self._ck(self.lib.erp_step(self.h, C.byref(st)))
+        self.last_stats = st.as_dict()
+        return bool(st.should_stop)
+
+    def step_host(self, x, y):
+        """Drop-in step for host-owned coordinates (float32 arrays, updated in place)."""
+        assert x.dtype == np.float32 and y.dtype == np.float32 and x.flags.c_contiguous
+        st = L.StepStats()
+        self._ck(self.lib.erp_step_host(self.h, x.ctypes.data_as(L.f32p), y.ctypes.data_as(L.f32p),
+                                        C.byref(st)))
+        return st.as_dict()
+
+    def run(self, max_iterations, stop_overflow=0.0):
+        it = C.c_int32()
+        st = L.StepStats()
+        self._ck(self.lib.erp_run(self.h, int(max_iterations), float(stop_overflow), C.byref(it),
+                                  C.byref(st)))
+        return int(it.value), st.as_dict()
+
+    def synchronize(self):
+        self._ck(self.lib.erp_synchronize(self.h))
+
+    def profile_stages(self, reps=10):
+        """Mean milliseconds per launch of each stage, timed in isolation with an
+        L2 flush before every launch (mutates the placement state)."""
+        out = (C.c_float * len(L.STAGES))()
+        self._ck(self.lib.erp_profile_stages(self.h, int(reps), out))
+        return dict(zip(L.STAGES, [float(v) for v in out]))
+
+    # -- state --
+    def scalars(self):
+        s = L.Scalars()
+        self._ck(self.lib.erp_get_scalars(self.h, C.byref(s)))
+        return s.as_dict()
+
+    def set_scalars(self, iteration, gamma, density_weight, alpha, beta):
+        self._ck(self.lib.erp_set_scalars(self.h, int(iteration), float(gamma), float(density_weight),
+                                          float(alpha), float(beta)))
+
+    def positions(self):
+        x = np.empty(self.N, np.float32)
+        y = np.empty(self.N, np.float32)
+        self._ck(self.lib.erp_get_positions(self.h, x.ctypes.data_as(L.f32p), y.ctypes.data_as(L.f32p)))
+        return x, y
+
+    def set_positions(self, x, y):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        self._ck(self.lib.erp_set_positions(self.h, x.ctypes.data_as(L.f32p), y.ctypes.data_as(L.f32p)))
+
+    def set_nesterov_history(self, px, py, pgx, pgy):
+        a = [np.ascontiguousarray(t, np.float32) for t in (px, py, pgx, pgy)]
+        self._ck(self.lib.erp_set_nesterov_history(self.h, *[t.ctypes.data_as(L.f32p) for t in a]))
+
+    def array(self, name):
+        which = L.ARR[name]
+        mn = self.m * self.n
+        if name == "DENSITY_I64":
+            out = np.empty(mn, np.int64)
+        elif name in ("PIN_GRAD_X", "PIN_GRAD_Y"):
+            out = np.empty(self.P, np.float32)
+        elif name == "NET_HPWL":
+            out = np.empty(self.E, np.float32)
+        elif name in ("DENSITY", "INITIAL", "FIELD_X", "FIELD_Y", "POTENTIAL"):
+            out = np.empty(mn, np.float32)
+        else:
+            out = np.empty(self.N, np.float32)
+        self._ck(self.lib.erp_get_array(self.h, which, out.ctypes.data_as(C.c_void_p), out.nbytes))
+        return out
+
+
+class SpectralSolver:
+    """Standalone Poisson solve (src/epotential.rs:284-343) on device pointers."""
+
+    def __init__(self, m, n, bin_w, bin_h, stream=None):
+        self.lib = L.load()
+        h = C.c_void_p()
+        L.check(self.lib.erp_spectral_create(int(m), int(n), float(bin_w), float(bin_h), L.PREC_FP32,
+                                             C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.h = h
+
+    def solve(self, rho_ptr, fx_ptr, fy_ptr, psi_ptr=None):
+        L.check(self.lib.erp_spectral_solve(self.h, C.c_void_p(rho_ptr), C.c_void_p(fx_ptr),
+                                            C.c_void_p(fy_ptr), C.c_void_p(psi_ptr) if psi_ptr else None))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.erp_spectral_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

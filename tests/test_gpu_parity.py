@@ -1,0 +1,200 @@
+"""GPU parity: every stage of the CUDA path, called through the C ABI, against
+the oracle on the same seeded inputs.
+
+Bars (per stage, identical inputs on both sides):
+  * integer work — the int64 fixed-point density map and the fixed-cell map —
+    bit-exact;
+  * WA pin/instance gradients, potential, fields, electric force: relative L2
+    <= 1e-5 (FP32);
+  * HPWL / overflow totals: relative 1e-6 (FP64 reductions on both sides);
+  * end to end after the same iteration count: HPWL within 0.5 %, overflow
+    within 0.005.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from designs import edge_design, small_synth, spread_positions
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def R(built):
+    import reda_erplacer_gb300 as R
+    return R
+
+
+@pytest.fixture(scope="module")
+def O(built):
+    from oracle import erp_oracle as O
+    return O
+
+
+def make_pair(R, O, d, m, n, td=1.0, xy=None):
+    o = O.Oracle(d, m, n, target_density=td, start_mode=O.START_DB, density_mode=O.DENSITY_FIXED,
+                 reduce_fp64=1)
+    g = R.Placement(d, (m, n), td, start_mode=1)
+    if xy is not None:
+        o.set_positions(*xy)
+        g.set_positions(*xy)
+    return o, g
+
+
+DESIGNS = {
+    "edge_32x16": (lambda: edge_design(), 32, 16),
+    "edge_16x64": (lambda: edge_design(seed=9), 16, 64),
+    "synth3k_64": (lambda: small_synth(3000, seed=11), 64, 64),
+    "synth20k_256": (lambda: small_synth(20000, seed=1, macros=0, io=400), 256, 256),
+}
+
+
+@pytest.fixture(scope="module", params=list(DESIGNS))
+def case(request, R, O):
+    mk, m, n = DESIGNS[request.param]
+    d = mk()
+    xy = spread_positions(d, seed=5, frac=0.6)
+    o, g = make_pair(R, O, d, m, n, xy=xy)
+    yield d, o, g, m, n
+    g.close()
+    o.close()
+
+
+def test_initial_density_bit_exact(case):
+    d, o, g, m, n = case
+    assert np.array_equal(g.array("INITIAL"), o.get("initial_map"))
+
+
+def test_wirelength(case):
+    d, o, g, m, n = case
+    for gamma in (0.5, 4.0, 40.0):
+        ho = o.compute_hpwl(gamma)
+        hg = g.compute_hpwl(gamma)
+        assert abs(hg - ho) <= 1e-6 * abs(ho)
+        assert rel_l2(g.array("PIN_GRAD_X"), o.get("pin_grad_x")) <= TOL
+        assert rel_l2(g.array("PIN_GRAD_Y"), o.get("pin_grad_y")) <= TOL
+        assert rel_l2(g.array("WL_GRAD_X"), o.get("wl_grad_x")) <= TOL
+        assert rel_l2(g.array("WL_GRAD_Y"), o.get("wl_grad_y")) <= TOL
+        assert np.allclose(g.array("NET_HPWL"), o.get("net_hpwl"), rtol=1e-6, atol=1e-6 * abs(ho))
+
+
+def test_potential(case):
+    d, o, g, m, n = case
+    eo, ovo = o.compute_potential(0)
+    eg, ovg = g.compute_potential(0)
+    assert np.array_equal(g.array("DENSITY_I64"), o.get("density_i64"))
+    assert np.array_equal(g.array("DENSITY"), o.get("density_map"))
+    assert abs(ovg - ovo) <= 1e-6 * max(abs(ovo), 1e-12)
+    assert rel_l2(g.array("FIELD_X"), o.get("field_x")) <= TOL
+    assert rel_l2(g.array("FIELD_Y"), o.get("field_y")) <= TOL
+    assert rel_l2(g.array("POTENTIAL"), o.get("potential")) <= TOL
+    assert abs(eg - eo) <= 1e-5 * abs(eo)
+    assert rel_l2(g.array("DENS_GRAD_X"), o.get("dens_grad_x")) <= TOL
+    assert rel_l2(g.array("DENS_GRAD_Y"), o.get("dens_grad_y")) <= TOL
+
+
+def test_nesterov_and_scheduler(case):
+    d, o, g, m, n = case
+    NM = d.num_movable
+    for it in (0, 1, 2):
+        hp_o = o.compute_hpwl(o.view().gamma)
+        hp_g = g.compute_hpwl(g.scalars()["gamma"])
+        _, ov_o = o.compute_potential(it)
+        _, ov_g = g.compute_potential(it)
+        x0, y0 = g.positions()
+        o.nesterov(it)
+        g.step_adaptive(it)
+        o.scheduler_update(hp_o, ov_o)
+        g.scheduler_update(hp_g, ov_g)
+        xg, yg = g.positions()
+        xo, yo = o.get("x"), o.get("y")
+        # compare the displacement of this step
+        assert rel_l2(xg[:NM] - x0[:NM], xo[:NM] - x0[:NM]) <= 1e-4
+        assert rel_l2(yg[:NM] - y0[:NM], yo[:NM] - y0[:NM]) <= 1e-4
+        s = g.scalars()
+        v = o.view()
+        assert s["iteration"] == v.iteration
+        for a, b in ((s["alpha"], v.alpha), (s["beta"], v.beta), (s["density_weight"], v.density_weight),
+                     (s["gamma"], v.gamma)):
+            assert abs(a - b) <= 1e-4 * abs(b) + 1e-12
+        # keep both sides on identical positions for the next round
+        o.set_positions(xg, yg)
+
+
+def test_step_matches_stage_sequence(R, O):
+    """erp_step (graph replay, on-device scheduler) == the stage entry points."""
+    d = small_synth(2000, seed=21)
+    a = R.Placement(d, (64, 64), 1.0, start_mode=1)
+    b = R.Placement(d, (64, 64), 1.0, start_mode=1)
+    for it in range(6):
+        a.step()
+        sa = a.last_stats
+        s = b.scalars()
+        hp = b.compute_hpwl(s["gamma"])
+        _, ov = b.compute_potential(it, want_energy=False)
+        b.step_adaptive(it)
+        b.scheduler_update(hp, ov)
+        assert abs(sa["hpwl"] - hp) <= 1e-6 * hp
+        assert abs(sa["overflow"] - ov) <= 1e-6
+    xa, ya = a.positions()
+    xb, yb = b.positions()
+    assert np.array_equal(xa, xb) and np.array_equal(ya, yb)
+
+
+def test_step_host_matches_step(R):
+    d = small_synth(2000, seed=22)
+    a = R.Placement(d, (64, 64), 1.0)
+    b = R.Placement(d, (64, 64), 1.0)
+    x, y = b.positions()
+    for _ in range(4):
+        a.step()
+        b.step_host(x, y)
+    xa, ya = a.positions()
+    assert np.array_equal(xa, x) and np.array_equal(ya, y)
+
+
+@pytest.mark.parametrize("iters", [150])
+def test_end_to_end_small(R, O, iters):
+    """Whole loop from the reference start (die centre) on the 20k-cell workload."""
+    d, cfg = R.workload_small()
+    o = O.Oracle(d, 256, 256, target_density=1.0, density_mode=O.DENSITY_FIXED, reduce_fp64=1)
+    g = R.Placement(d, (256, 256), 1.0)
+    for i in range(iters):
+        so = o.step()
+        g.step()
+        sg = g.last_stats
+        assert abs(sg["hpwl"] - so["hpwl"]) <= 0.005 * so["hpwl"], (i, sg, so)
+        assert abs(sg["overflow"] - so["overflow"]) <= 0.005, (i, sg, so)
+
+
+def test_run_retires_at_overflow(R):
+    d = small_synth(3000, seed=23)
+    g = R.Placement(d, (64, 64), 1.0)
+    it, last = g.run(400, stop_overflow=0.3)
+    assert last["overflow"] <= 0.3
+    assert it == last["iteration"] + 1
+    # a second run continues from there
+    it2, last2 = g.run(3, 0.0)
+    assert it2 == 3 and last2["iteration"] == last["iteration"] + 3
+
+
+def test_spectral_standalone_fp64_error(R, O):
+    """Isolated Poisson solve at 512x512 against the FP64 solve (error reported)."""
+    import torch
+    rng = np.random.default_rng(3)
+    m = n = 512
+    rho = (0.7 + 0.3 * rng.random((m, n))).astype(np.float64)
+    bw, bh = 1.3, 1.1
+    fx64, fy64, p64 = O.poisson(rho, bw, bh, dtype=np.float64)
+    sol = R.SpectralSolver(m, n, bw, bh)
+    r = torch.tensor(rho.astype(np.float32), device="cuda")
+    fx = torch.empty_like(r); fy = torch.empty_like(r); ps = torch.empty_like(r)
+    sol.solve(r.data_ptr(), fx.data_ptr(), fy.data_ptr(), ps.data_ptr())
+    torch.cuda.synchronize()
+    ex = rel_l2(fx.cpu().numpy(), fx64)
+    ey = rel_l2(fy.cpu().numpy(), fy64)
+    ep = rel_l2(ps.cpu().numpy(), p64)
+    print(f"FP32 FFT solve vs FP64: field_x {ex:.2e} field_y {ey:.2e} potential {ep:.2e}")
+    assert max(ex, ey, ep) <= 1e-5
