@@ -23,10 +23,8 @@ def rel_l2(a, b):
 @pytest.fixture(scope="session")
 def built():
     """Build the product library and the oracle (both in-tree)."""
-    from reda_erplacer_gb300 import build as B
-    B.build()
-    from oracle import build_oracle
-    build_oracle.build()
+    import __graft_entry__
+    __graft_entry__.build()
     return True
 
 

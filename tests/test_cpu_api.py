@@ -1,0 +1,124 @@
+"""CPU-only checks of the C ABI library: it loads, exports every symbol that
+include/erplacer.h declares, rejects bad designs, fails loudly without a GPU,
+and its synthetic netlist generator follows its documented rule."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, gpu_available
+from designs import build_design, edge_design
+
+
+@pytest.fixture(scope="module")
+def R(built):
+    import reda_erplacer_gb300 as R
+    return R
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "erplacer.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(erp_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol(R):
+    lib = C.CDLL(R.lib.LIB_PATH)
+    syms = declared_symbols()
+    assert len(syms) >= 25
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    # the Python binding covers the whole header as well
+    assert set(syms) <= set(R.lib.EXPORTS)
+
+
+def test_status_strings(R):
+    assert R.lib.status_string(0) == "ok"
+    assert "sm_103" in R.lib.status_string(7)
+    assert R.lib.load().erp_abi_version() == 1
+
+
+@pytest.mark.skipif(gpu_available(), reason="checks the no-GPU failure path")
+def test_no_gpu_fails_loudly(R):
+    d = edge_design()
+    with pytest.raises(R.ErpError) as e:
+        R.Placement(d, (32, 16), 1.0)
+    assert e.value.status == R.lib.ENODEV
+
+
+def test_invalid_designs_rejected(R):
+    d = edge_design()
+    bad = [("bins not power of two", dict(num_bins=(30, 16))),
+           ("bins too small", dict(num_bins=(8, 16)))]
+    for _, kw in bad:
+        with pytest.raises(R.ErpError) as e:
+            R.Placement(d, **kw)
+        assert e.value.status == R.lib.EINVAL
+    # a pin in two nets
+    d2 = edge_design()
+    d2.net_pins = d2.net_pins.copy()
+    d2.net_pins[1] = d2.net_pins[0]
+    with pytest.raises(R.ErpError) as e:
+        R.Placement(d2, (32, 16))
+    assert e.value.status == R.lib.EINVAL and "more than one net" in str(e.value)
+    # n_2nets claims a 3-pin net
+    d3 = edge_design()
+    d3.n_2nets = d3.n_2nets + 10
+    with pytest.raises(R.ErpError) as e:
+        R.Placement(d3, (32, 16))
+    assert e.value.status == R.lib.EINVAL
+
+
+def test_synth_is_deterministic_and_follows_rule(R):
+    a = R.synth(5000, 5250, num_io=100, num_macros=4, utilization=0.65, seed=42)
+    b = R.synth(5000, 5250, num_io=100, num_macros=4, utilization=0.65, seed=42)
+    c = R.synth(5000, 5250, num_io=100, num_macros=4, utilization=0.65, seed=43)
+    for k in ("x", "y", "w", "h", "pin_ox", "pin_inst", "net_ptr", "net_pins"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    assert not np.array_equal(a.pin_inst, c.pin_inst)
+    NM = a.num_movable
+    assert NM == 5000 and a.num_nodes == 5000 + 4 + 100 and a.num_nets == 5250
+    deg = np.diff(a.net_ptr)
+    # exact class shares; the rounding remainder goes to the two-pin class
+    assert abs(a.n_2nets - 0.55 * 5250) <= 2 and np.all(deg[: a.n_2nets] == 2)
+    assert np.all(deg[a.n_2nets:] >= 3) and deg.max() <= 128 + 100
+    # widths are integer multiples of the 0.2 um site in [2, 16] sites, one row high
+    sites = a.w[:NM] / 0.2
+    assert np.allclose(sites, np.round(sites), atol=1e-4) and sites.min() >= 2 - 1e-4 and sites.max() <= 16 + 1e-4
+    assert np.all(a.h[:NM] == 2.0)
+    # distinct cells per net
+    for e in range(a.num_nets):
+        pins = a.net_pins[a.net_ptr[e]:a.net_ptr[e + 1]]
+        insts = a.pin_inst[pins]
+        assert len(set(insts.tolist())) == len(insts)
+    # IO pins sit on the boundary with zero size
+    io = slice(NM + 4, a.num_nodes)
+    on_edge = (a.x[io] == 0) | (a.y[io] == 0) | np.isclose(a.x[io], a.die_w) | np.isclose(a.y[io], a.die_h)
+    assert np.all(on_edge) and np.all(a.w[io] == 0)
+    # utilisation of the free area
+    free = a.die_w * a.die_h - np.sum(a.w[NM:NM + 4].astype(np.float64) * a.h[NM:NM + 4])
+    assert a.cell_utilization == pytest.approx(a.movable_area / free, rel=1e-5)
+    assert a.cell_utilization == pytest.approx(0.65, rel=1e-3)
+    # macros do not overlap
+    mx = [(a.x[i], a.y[i], a.w[i], a.h[i]) for i in range(NM, NM + 4)]
+    for i in range(4):
+        for j in range(i + 1, 4):
+            xi, yi, wi, hi = mx[i]
+            xj, yj, wj, hj = mx[j]
+            assert xi + wi <= xj + 1e-3 or xj + wj <= xi + 1e-3 or yi + hi <= yj + 1e-3 or yj + hj <= yi + 1e-3
+
+
+def test_bins_for_cells_rule(R):
+    assert R.bins_for_cells(2000) == 64       # sqrt(2000)/2 = 22 -> 32 -> clamp 64
+    assert R.bins_for_cells(200000) == 256    # 223.6 -> 256
+    assert R.bins_for_cells(5_000_000) == 1024
+
+
+def test_design_struct_roundtrip(R):
+    d = edge_design()
+    s = d.to_struct()
+    back = R.Design.from_struct(s)
+    for k in ("x", "pin_inst", "net_ptr", "net_pins", "inst_pin_ptr", "inst_pins"):
+        assert np.array_equal(getattr(back, k), getattr(d, k))

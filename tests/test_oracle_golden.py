@@ -1,0 +1,181 @@
+"""Pin the oracle against the FP64 golden fixtures (tests/golden/make_golden.py)
+and against the reference's documented quirks.  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from designs import build_design
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def O(built):
+    from oracle import erp_oracle as O
+    return O
+
+
+@pytest.mark.parametrize("shape", ["16x16", "16x32", "64x32"])
+@pytest.mark.parametrize("name", ["dct2", "idct2", "idct_idxst", "idxst_idct"])
+def test_transforms_vs_closed_form(O, name, shape):
+    g = np.load(os.path.join(GOLD, "spectral_golden.npz"))
+    x, want = g[f"x_{shape}"], g[f"{name}_{shape}"]
+    assert rel_l2(O.transform(name, x, np.float64), want) <= 1e-12
+    assert rel_l2(O.transform(name, x.astype(np.float32), np.float32), want) <= 2e-6
+
+
+def test_poisson_vs_closed_form(O):
+    g = np.load(os.path.join(GOLD, "spectral_golden.npz"))
+    bw, bh = g["poisson_bins"]
+    fx, fy, psi = O.poisson(g["poisson_rho"], bw, bh, np.float64)
+    assert rel_l2(fx, g["poisson_fx"]) <= 1e-12
+    assert rel_l2(fy, g["poisson_fy"]) <= 1e-12
+    assert rel_l2(psi, g["poisson_psi"]) <= 1e-12
+    fx, fy, psi = O.poisson(g["poisson_rho"].astype(np.float32), bw, bh, np.float32)
+    for a, b in ((fx, "poisson_fx"), (fy, "poisson_fy"), (psi, "poisson_psi")):
+        assert rel_l2(a, g[b]) <= 5e-6
+
+
+def _wa_design():
+    g = np.load(os.path.join(GOLD, "wa_golden.npz"))
+    net_ptr, net_pins = g["net_ptr"], g["net_pins"]
+    nets = [list(net_pins[net_ptr[e]:net_ptr[e + 1]]) for e in range(len(net_ptr) - 1)]
+    d = build_design(g["x"], g["y"], g["w"], g["h"], len(g["x"]), nets, g["pin_inst"], g["pin_ox"],
+                     g["pin_oy"], float(g["die"][0]), float(g["die"][1]), int(g["n_2nets"][0]))
+    return d, g
+
+
+def test_wirelength_vs_analytic(O):
+    d, g = _wa_design()
+    o = O.Oracle(d, 16, 16, target_density=1.0, start_mode=O.START_DB)
+    for gamma in g["gammas"]:
+        hp = o.compute_hpwl(float(gamma))
+        assert rel_l2(o.get("pin_grad_x"), g[f"grad_x_{gamma}"]) <= 5e-6
+        assert rel_l2(o.get("pin_grad_y"), g[f"grad_y_{gamma}"]) <= 5e-6
+        assert rel_l2(o.get("net_hpwl"), g[f"hpwl_{gamma}"]) <= 1e-6
+        assert abs(hp - g[f"hpwl_{gamma}"].sum()) <= 1e-6 * hp
+        # instance gradient = sum of its pins (src/hpwl.rs:113-135)
+        want = np.zeros(d.num_nodes)
+        np.add.at(want, d.pin_inst, o.get("pin_grad_x"))
+        assert rel_l2(o.get("wl_grad_x"), want) <= 1e-6
+
+
+def _density_design():
+    g = np.load(os.path.join(GOLD, "density_golden.npz"))
+    X = np.concatenate([g["x"], g["fx"]])
+    Y = np.concatenate([g["y"], g["fy"]])
+    W = np.concatenate([g["w"], g["fw"]])
+    H = np.concatenate([g["h"], g["fh"]])
+    d = build_design(X, Y, W, H, len(g["x"]), [], [], [], [], float(g["die"][0]), float(g["die"][1]), 0)
+    return d, g
+
+
+@pytest.mark.parametrize("mode", ["fixed", "reference"])
+def test_density_vs_exact_overlap(O, mode):
+    d, g = _density_design()
+    m, n = (int(v) for v in g["bins"])
+    o = O.Oracle(d, m, n, target_density=float(g["td"][0]), start_mode=O.START_DB,
+                 density_mode=O.DENSITY_FIXED if mode == "fixed" else O.DENSITY_REFERENCE)
+    assert rel_l2(o.get("initial_map"), g["initial"].ravel()) <= 1e-6
+    for it in (0, 250):   # both reference density variants (src/epotential.rs:245)
+        _, ovf = o.compute_potential(it)
+        dm = o.get("density_map").reshape(m, n)
+        assert rel_l2(dm, g["density_scaled"]) <= 1e-6
+        # quirk: the last bin row / column never receive density (src/density.rs:71,80,209,218)
+        assert np.all(dm[m - 1, :] == 0) and np.all(dm[:, n - 1] == 0)
+        assert abs(ovf - g["overflow"][0]) <= 1e-5 * g["overflow"][0]
+
+
+def test_fixed_point_replay_matches_float_sums(O):
+    from reda_erplacer_gb300 import synth
+    d = synth(3000, 3150, num_io=40, num_macros=3, utilization=0.7, seed=4)
+    a = O.Oracle(d, 64, 64, target_density=1.0, density_mode=O.DENSITY_FIXED)
+    b = O.Oracle(d, 64, 64, target_density=1.0, density_mode=O.DENSITY_REFERENCE, num_threads=1)
+    a.compute_potential(0)
+    b.compute_potential(0)
+    assert rel_l2(a.get("density_map"), b.get("density_map")) <= 1e-6
+    assert rel_l2(a.get("initial_map"), b.get("initial_map")) <= 1e-6
+    assert rel_l2(a.get("field_x"), b.get("field_x")) <= 1e-5
+    # the integer map is exact: the same sum in any order
+    s = a.get("density_i64")
+    assert s.dtype == np.int64 and s.min() >= 0
+
+
+def test_fixed_shift_rule(O):
+    assert O.fixed_shift(1.0) == 60          # 1 < 2^1
+    assert O.fixed_shift(3.6e6) == 61 - 22   # 2^21 <= 3.6e6 < 2^22
+    assert O.fixed_shift(0.0) == 61
+
+
+def test_scheduler_known_answers(O):
+    d, _ = _wa_design()
+    o = O.Oracle(d, 16, 16, target_density=1.0, start_mode=O.START_DB, reduce_fp64=0)
+    v = o.view()
+    bw, bh = v.bin_w, v.bin_h
+    assert v.gamma == pytest.approx(4.0 * (bw + bh))            # src/scheduler.rs:56
+    assert v.density_weight == pytest.approx(8e-5)              # src/scheduler.rs:57
+    o.scheduler_update(100.0, 0.1)     # first update: delta = 100 - 0 >= 0
+    v = o.view()
+    # power = clamp(1.05^(-100/100), .95, 1.05) = 0.95238; mu = 1.05 * power = 1.0
+    assert v.density_weight == pytest.approx(8e-5 * 1.05 * 1.05 ** -1, rel=1e-6)
+    # gamma coefficient 10^((0.1-0.1)*20/9 - 1) = 0.1
+    assert v.gamma == pytest.approx(0.1 * 4.0 * (bw + bh), rel=1e-6)
+    o.scheduler_update(50.0, 2.0)      # delta < 0: power = max(0.9999^2, 0.98)
+    v = o.view()
+    assert v.density_weight == pytest.approx(8e-5 * 1.0 * 1.05 * 0.9999 ** 2, rel=1e-5)
+    assert v.gamma == pytest.approx(10.0 * 4.0 * (bw + bh), rel=1e-6)   # clamped at 10
+    assert not o.view().hpwl_initial_set == 0
+
+
+def test_nesterov_momentum_and_clamp(O):
+    d, _ = _wa_design()
+    o = O.Oracle(d, 16, 16, target_density=1.0, start_mode=O.START_DB)
+    o.compute_hpwl(3.0)
+    o.compute_potential(0)
+    o.nesterov(0)
+    v = o.view()
+    a1 = (1 + np.sqrt(4 * 1.0 + 1)) / 2                      # src/nesterov.rs:148-158
+    assert v.alpha == pytest.approx(a1, rel=1e-6) and v.beta == 0.0
+    x = o.get("x")[: d.num_movable]
+    assert np.all(x >= 0) and np.all(x <= d.die_w - d.w[: d.num_movable] - 1)
+
+
+def test_literal_and_fp64_modes_track(O):
+    """The documented FP64 reductions / fixed-point density (used by the GPU
+    path) follow the reference's literal FP32 loop: after the same iteration
+    count HPWL within 0.5 % and overflow within 0.005, from the jittered start.
+    (From the reference's exact-centre start the iteration-0 density-weight
+    rescale divides by a force that is pure rounding noise, so no two
+    summation orders agree there; see test_center_start_rescale_is_noise.)"""
+    from reda_erplacer_gb300 import synth
+    d = synth(3000, 3150, num_io=40, num_macros=0, utilization=0.7, seed=9)
+    a = O.Oracle(d, 64, 64, target_density=1.0, start_mode=O.START_DB,
+                 density_mode=O.DENSITY_FIXED, reduce_fp64=1)
+    b = O.Oracle(d, 64, 64, target_density=1.0, start_mode=O.START_DB,
+                 density_mode=O.DENSITY_REFERENCE, reduce_fp64=0, num_threads=1)
+    rel = []
+    for i in range(60):
+        sa, sb = a.step(), b.step()
+        rel.append(abs(sa["hpwl"] - sb["hpwl"]) / sb["hpwl"])
+    assert rel[-1] <= 5e-3 and abs(sa["overflow"] - sb["overflow"]) <= 5e-3
+    assert float(np.median(rel)) <= 2e-3
+
+
+def test_center_start_rescale_is_noise(O):
+    """At the reference start every movable cell sits at the die centre: the map
+    is symmetric, the density force is rounding noise, and the iteration-0
+    density-weight rescale (src/nesterov.rs:47-55) differs between two exact-
+    to-rounding evaluations by far more than rounding."""
+    from reda_erplacer_gb300 import synth
+    d = synth(3000, 3150, num_io=40, num_macros=0, utilization=0.7, seed=9)
+    a = O.Oracle(d, 64, 64, target_density=1.0, density_mode=O.DENSITY_FIXED, reduce_fp64=1)
+    b = O.Oracle(d, 64, 64, target_density=1.0, density_mode=O.DENSITY_REFERENCE, reduce_fp64=0,
+                 num_threads=1)
+    sa, sb = a.step(), b.step()
+    assert sa["hpwl"] == pytest.approx(sb["hpwl"], rel=1e-6)
+    # ~3000 FP32 contributions summed sequentially into the centre bins
+    assert rel_l2(a.get("density_map"), b.get("density_map")) <= 1e-5
+    ratio = a.view().density_weight / b.view().density_weight
+    assert ratio > 1.1 or ratio < 0.9
