@@ -151,7 +151,7 @@ def cpu_sample(d, cfg, iters, literal):
     """Time `iters` oracle steps (all host threads) after one untimed step."""
     from oracle import erp_oracle as O
     m, n = cfg["bins"]
-    o = O.Oracle(d, m, n, target_density=cfg["target_density"],
+    o = O.Oracle(d, m, n, target_density=cfg["target_density"], start_mode=O.START_DB,
                  density_mode=O.DENSITY_REFERENCE if literal else O.DENSITY_FIXED,
                  reduce_fp64=0 if literal else 1, num_threads=0)
     o.step()
@@ -199,7 +199,8 @@ def run_ours(args):
     d, cfg, desc = make_workload(args.workload)
     m, n = cfg["bins"]
     stream = torch.cuda.Stream()
-    pl = R.Placement(d, (m, n), cfg["target_density"], device=local, stream=stream.cuda_stream)
+    pl = R.Placement(d, (m, n), cfg["target_density"], start_mode=1, device=local,
+                     stream=stream.cuda_stream)
     for _ in range(args.warmup):
         pl.step(stats=False)
     pl.synchronize()
@@ -223,6 +224,12 @@ def run_ours(args):
     st = pl.scalars()
     x_h, y_h = pl.positions()
     value = world * args.steps / (ms / 1000.0)
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms / args.steps,
+                              "graph_kernels": st["graph_kernels"], "quick": True}), flush=True)
+        pl.close()
+        return 0
 
     # end to end through the drop-in host-coordinate call, pinned buffers
     N = d.num_nodes
@@ -261,7 +268,8 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": desc, "cells": d.num_movable, "nets": d.num_nets,
                    "pins": d.num_pins, "bins": [m, n], "target_density": cfg["target_density"],
-                   "start": "reference rule (die centre)", "parallelism": f"replicas x{world}",
+                   "start": "die centre + Gaussian jitter (sigma 0.1% of die width)",
+                   "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (per-step working set > 129 MiB), no flush",
                    "iteration_after": sc["iteration"], "hpwl_after": sc["hpwl_current"],
                    "overflow_after": sc["overflow_current"]},
@@ -295,6 +303,7 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--ref-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="timed steps only (for profiler runs)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

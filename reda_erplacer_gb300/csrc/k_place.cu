@@ -186,10 +186,17 @@ __device__ __forceinline__ float tri_clamped(float x, float s, int k, float bs) 
 
 // compute_density_overflow_map_sequential's bin range and per-(cell, bin)
 // contribution (src/density.rs:195-229), accumulated as rint(v * 2^S) into an
-// int64 map.  Lanes of a warp walk their contributions in lock-step; lanes that
-// hit the same bin combine their integers first (one atomic per distinct bin
-// per warp step), which removes the hot-spot serialisation of the early
-// iterations when all cells sit at the die centre.
+// int64 map.  Integer sums are order independent, so the privatisation below
+// changes no bit of the result:
+//  * lanes of a warp walk their contributions in lock-step; lanes that hit the
+//    same bin combine their integers first (one atomic per distinct bin per
+//    warp step);
+//  * each block owns a kWin x kWin bin window in shared memory anchored at its
+//    first cell; contributions inside it are accumulated there and flushed with
+//    one global atomic per touched bin, the rest go to global memory directly.
+// Early on all cells sit within a few bins of the die centre, where this turns
+// millions of contended global atomics into a few per block.
+constexpr int kWin = 64;
 __global__ void __launch_bounds__(kThreads) k_density_scatter(
     int NM, const float *__restrict__ x, const float *__restrict__ y,
     const float *__restrict__ offx, const float *__restrict__ offy, const float *__restrict__ cw,
@@ -197,14 +204,30 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
     float bh, float inv_bw, float inv_bh, float scale, unsigned long long *__restrict__ map,
     const DevState *__restrict__ st) {
     __shared__ long long sh[kThreads];
+    __shared__ unsigned long long win[kWin * kWin];
+    __shared__ int s_org[2];
     if (st->done) return;
     const int lane = threadIdx.x & 31;
     const int wbase = threadIdx.x & ~31;
-    for (int base = blockIdx.x * blockDim.x; base < NM; base += gridDim.x * blockDim.x) {
+    const int per = ((NM + gridDim.x - 1) / gridDim.x + 31) & ~31;
+    const int c0 = blockIdx.x * per, c1 = min(c0 + per, NM);
+    if (threadIdx.x == 0) {
+        int ox = 0, oy = 0;
+        if (c0 < NM) {
+            ox = (int)floorf(clamp_bin((x[c0] + offx[c0]) * inv_bw, m)) - kWin / 2;
+            oy = (int)floorf(clamp_bin((y[c0] + offy[c0]) * inv_bh, n)) - kWin / 2;
+        }
+        s_org[0] = max(0, min(ox, m - kWin));
+        s_org[1] = max(0, min(oy, n - kWin));
+    }
+    for (int k = threadIdx.x; k < kWin * kWin; k += blockDim.x) win[k] = 0ull;
+    __syncthreads();
+    const int wox = s_org[0], woy = s_org[1];
+    for (int base = c0; base < c1; base += blockDim.x) {
         const int i = base + threadIdx.x;
         int bxl = 0, byl = 0, nx = 0, ny = 0;
         float xi = 0.f, yi = 0.f, sxi = 0.f, syi = 0.f, r = 0.f;
-        if (i < NM) {
+        if (i < c1) {
             xi = x[i] + offx[i];
             yi = y[i] + offy[i];
             sxi = cw[i];
@@ -239,10 +262,23 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
             if (key >= 0 && lane == __ffs(peers) - 1) {
                 long long s = 0;
                 for (unsigned p = peers; p; p &= p - 1) s += sh[wbase + __ffs(p) - 1];
-                if (s) atomicAdd(map + key, (unsigned long long)s);
+                if (s) {
+                    const int bx = key / n, by = key - bx * n;
+                    const int wx = bx - wox, wy = by - woy;
+                    if (wx >= 0 && wx < kWin && wy >= 0 && wy < kWin)
+                        atomicAdd(win + wx * kWin + wy, (unsigned long long)s);
+                    else
+                        atomicAdd(map + key, (unsigned long long)s);
+                }
             }
             __syncwarp();
         }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kWin * kWin; k += blockDim.x) {
+        const unsigned long long v = win[k];
+        const int bx = wox + k / kWin, by = woy + k % kWin;
+        if (v && bx < m && by < n) atomicAdd(map + (size_t)bx * n + by, v);
     }
 }
 
@@ -548,7 +584,7 @@ void launch_wl_gather(Ctx &c) {
 }
 
 void launch_density_scatter(Ctx &c) {
-    k_density_scatter<<<grid_for(c.NM, 152 * 16), kThreads, 0, c.stream>>>(
+    k_density_scatter<<<grid_for(c.NM, 152 * 4), kThreads, 0, c.stream>>>(
         c.NM, c.x, c.y, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw,
         c.inv_bh, c.fixed_scale, c.dmap, c.st);
 }
