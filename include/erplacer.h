@@ -230,6 +230,23 @@ erp_status erp_spectral_solve(erp_spectral *sp, const float *rho_dev, float *fie
                               float *field_y_dev, float *potential_dev);
 void erp_spectral_destroy(erp_spectral *sp);
 
+/* Allocation-free form of erp_spectral_create + erp_spectral_solve, for callers
+ * that cannot call cudaMalloc: hosts whose device memory belongs to another
+ * allocator's pool (a framework caching allocator, a pre-reserved arena) and
+ * loops that must not stall on cudaFree's device-wide synchronisation.  It has
+ * no counterpart in the reference.  All intermediates live in one file-scope
+ * device array of about 4.1 MiB that every GPU loading the library holds until
+ * exit; grids above ERP_NOALLOC_MAX_BINS (the reference's 512 x 512) are
+ * rejected with ERP_EINVAL.  The caller passes device buffers of m*n floats
+ * (potential may be NULL) and a stream (NULL: the legacy default stream).
+ * The first call on a device looks up the array's address and sets kernel
+ * limits: make it before any stream capture.  Every call reuses the array, so
+ * calls that overlap on the GPU race; sequential calls are independent. */
+#define ERP_NOALLOC_MAX_BINS (512 * 512)
+erp_status erp_spectral_solve_noalloc(int32_t m, int32_t n, float bin_w, float bin_h,
+                                      const float *rho_dev, float *field_x_dev,
+                                      float *field_y_dev, float *potential_dev, void *stream);
+
 /* ---- seeded synthetic netlists (stand-in for reda-db's read_db on the
  * LEF/DEF benchmarks, which are not shipped) ---- */
 typedef struct erp_synth_params {

@@ -24,6 +24,7 @@ CU_SOURCES = {
     "k_place.cu": ["-fmad=false"],
     "k_spectral.cu": [],
     "erp_api.cu": [],
+    "erp_noalloc.cu": [],
 }
 CPP_SOURCES = ["synth.cpp"]
 HEADERS = ["erp_internal.cuh", "reduce.cuh"]

@@ -25,6 +25,8 @@ struct erp_spectral {
 
 static thread_local std::string g_create_err;
 
+void erp::set_thread_error(const std::string &msg) { g_create_err = msg; }
+
 extern "C" const char *erp_status_string(erp_status s) {
     switch (s) {
     case ERP_OK: return "ok";

@@ -151,6 +151,9 @@ size_t spectral_smem_bytes(int m, int n);
 
 int ilog2(int v);
 
+// Message returned by erp_last_error(NULL) on this host thread.
+void set_thread_error(const std::string &msg);
+
 }  // namespace erp
 
 #define ERP_CUDA_CHECK_RET(c, expr)                                                  \

@@ -98,6 +98,8 @@ EXPORTS = {
                                       C.c_void_p, C.POINTER(C.c_void_p)]),
     "erp_spectral_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "erp_spectral_destroy": (None, [C.c_void_p]),
+    "erp_spectral_solve_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_void_p,
+                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "erp_synth_create": (C.c_int, [C.POINTER(SynthParams), C.POINTER(C.c_void_p)]),
     "erp_synth_design": (C.c_int, [C.c_void_p, C.POINTER(Design)]),
     "erp_synth_destroy": (None, [C.c_void_p]),
