@@ -297,6 +297,348 @@ __global__ void __launch_bounds__(kThreads) k_rows_inv(
     }
 }
 
+// ===================================================================
+// Warp-level four-step FFT for N = 32 * E points (E = 1..32), one warp per
+// complex sequence: lane l holds r[k] = z[l + 32k].
+//   1. E-point DIF FFT in registers over k        (twiddles W_E = W_N^32)
+//   2. twiddle W_N^(l*q)
+//   3. 32-point DIF across lanes with xor shuffles (twiddles W_32 = W_N^E)
+// after which lane l, register j holds Z[brev_E(j) + E * brev_5(l)].  The
+// result is staged in shared memory in natural order under an XOR swizzle
+// (index f -> f ^ ((f >> 5) & 31)) that keeps both the scattered store and the
+// row-order reads at two wavefronts per 64-bit warp access.
+// ===================================================================
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ int swz(int f) { return f ^ ((f >> 5) & 31); }
+
+template <int E>
+__host__ __device__ constexpr int brev_c(int v) {
+    int r = 0;
+    for (int b = 1; b < E; b <<= 1) r = (r << 1) | ((v & b) ? 1 : 0);
+    return r;
+}
+
+template <int E, bool INV>
+__device__ __forceinline__ void warp_fft(float2 (&r)[E], const float2 *__restrict__ tw, int lane) {
+    constexpr int N = 32 * E;
+    // 1. registers
+#pragma unroll
+    for (int h = E / 2; h >= 1; h >>= 1) {
+#pragma unroll
+        for (int i0 = 0; i0 < E; ++i0) {
+            if (i0 & h) continue;
+            const int i1 = i0 + h, j = i0 & (h - 1);
+            float2 w = tw[32 * j * (E / (2 * h))];
+            if (INV) w.y = -w.y;
+            const float2 u = r[i0], v = r[i1];
+            r[i0] = make_float2(u.x + v.x, u.y + v.y);
+            r[i1] = cmulf(make_float2(u.x - v.x, u.y - v.y), w);
+        }
+    }
+    // 2. twiddles
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+        const int q = brev_c<E>(j);
+        if (q == 0) continue;
+        const int idx = lane * q;
+        float2 w = idx < N / 2 ? tw[idx] : tw[idx - N / 2];
+        if (idx >= N / 2) { w.x = -w.x; w.y = -w.y; }
+        if (INV) w.y = -w.y;
+        r[j] = cmulf(r[j], w);
+    }
+    // 3. across lanes
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+        const int h = 16 >> s;
+        const bool upper = (lane & h) != 0;
+        float2 w = tw[E * ((lane & (h - 1)) * (16 / h))];
+        if (INV) w.y = -w.y;
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+            const float2 v = r[j];
+            const float2 p = make_float2(__shfl_xor_sync(0xffffffffu, v.x, h),
+                                         __shfl_xor_sync(0xffffffffu, v.y, h));
+            r[j] = upper ? cmulf(make_float2(p.x - v.x, p.y - v.y), w) : make_float2(v.x + p.x, v.y + p.y);
+        }
+    }
+}
+
+// stage the FFT result in natural (swizzled) order
+template <int E>
+__device__ __forceinline__ void warp_fft_store(const float2 (&r)[E], float2 *buf, int lane) {
+    const int pl = (int)(__brev((unsigned)lane) >> 27);
+#pragma unroll
+    for (int j = 0; j < E; ++j) buf[swz(brev_c<E>(j) + E * pl)] = r[j];
+}
+
+// Block-cooperative staging of the per-axis tables in shared memory: the
+// half-size FFT's twiddles e^{-2 pi i k / H} = tw_N[2k] (k < H/2), the N-point
+// twiddles tw_N (k < N/2) and the DCT post-twiddles ek (k < N), N = 2H.
+struct AxisTables {
+    float2 *twh, *tw, *ek;
+};
+template <int NW, int H>
+__device__ __forceinline__ AxisTables load_tables(float2 *base, const float2 *__restrict__ tw_g,
+                                                  const float2 *__restrict__ ek_g) {
+    AxisTables t;
+    t.twh = base;
+    t.tw = base + H / 2;
+    t.ek = base + H / 2 + H;
+    for (int k = threadIdx.x; k < H / 2; k += NW * 32) t.twh[k] = tw_g[2 * k];
+    for (int k = threadIdx.x; k < H; k += NW * 32) t.tw[k] = tw_g[k];
+    for (int k = threadIdx.x; k < 2 * H; k += NW * 32) t.ek[k] = ek_g[k];
+    return t;
+}
+template <int H>
+constexpr int tables_f2() { return H / 2 + H + 2 * H; }
+
+// Real DCT-II of the N = 2H values staged at their Makhoul positions in xm
+// (v[p] at xm[p]): one H-point complex FFT over z[j] = v[2j] + i v[2j+1], then
+// V[k] = E[k] + W_N^k O[k] and y[k] = Re(e^{-i pi k / 2N} V[k]).  Calls emit(k, y)
+// for every k in [0, N), each exactly once across the warp.
+template <int E, typename Emit>
+__device__ __forceinline__ void warp_dct2_real(const float *xm, float2 *zb, const float2 *twh,
+                                               const float2 *tw_n, const float2 *ek, int lane, Emit emit) {
+    constexpr int H = 32 * E, N = 2 * H;
+    float2 r[E];
+    const float2 *xm2 = reinterpret_cast<const float2 *>(xm);
+#pragma unroll
+    for (int k = 0; k < E; ++k) r[k] = xm2[lane + 32 * k];
+    warp_fft<E, false>(r, twh, lane);
+    warp_fft_store<E>(r, zb, lane);
+    __syncwarp();
+    for (int k = lane; k <= H; k += 32) {
+        const float2 zk = zb[swz(k & (H - 1))];
+        float2 zc = zb[swz((H - k) & (H - 1))];
+        zc.y = -zc.y;
+        const float2 ev = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
+        const float2 od = make_float2(0.5f * (zk.y - zc.y), -0.5f * (zk.x - zc.x));
+        const float2 w = k < H ? tw_n[k] : make_float2(-1.0f, 0.0f);
+        const float2 v = make_float2(ev.x + (w.x * od.x - w.y * od.y), ev.y + (w.x * od.y + w.y * od.x));
+        const float2 e = ek[k];
+        emit(k, e.x * v.x - e.y * v.y);
+        if (k > 0 && k < H) {
+            const float2 e2 = ek[N - k];
+            emit(N - k, e2.x * v.x + e2.y * v.y);
+        }
+    }
+}
+
+// Inverse along one axis of N = 2H real values, IDCT (sine = false) or IDXST
+// (sine = true): x(u) returns X[u] for u in [0, N) (the caller's weighted
+// input); the Hermitian spectrum Vi is folded into one H-point complex IFFT
+// (Fe = Vi[k] + Vi[k+H], Fo = (Vi[k] - Vi[k+H]) e^{+2 pi i k / N}), whose real
+// and imaginary parts are w[2j] and w[2j+1].  Calls emit(i, out_i) for every
+// output index i in [0, N), each exactly once across the warp.
+template <int E, typename XFn, typename Emit>
+__device__ __forceinline__ void warp_inv_real(XFn x, bool sine, float2 *zb, const float2 *twh,
+                                              const float2 *tw_n, const float2 *ek, int lane, Emit emit) {
+    constexpr int H = 32 * E, N = 2 * H;
+    float2 r[E];
+#pragma unroll 1
+    for (int t = 0; t < E; ++t) {
+        const int k = lane + 32 * t;
+        float2 v[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int u = k + h * H;
+            const int un = N - u;   // in (0, N]; X[N] := 0
+            const float xu = x(u);
+            const float xn = (un == N) ? 0.0f : x(un);
+            if (!sine) v[h] = idct_spec(xu, xn, ek[u]);
+            else v[h] = (u == 0) ? make_float2(0.f, 0.f) : idct_spec(xn, xu, ek[u]);
+        }
+        const float2 fe = make_float2(v[0].x + v[1].x, v[0].y + v[1].y);
+        const float2 d = make_float2(v[0].x - v[1].x, v[0].y - v[1].y);
+        const float2 w = tw_n[k];   // e^{-2 pi i k / N}; Fo = d * conj(w)
+        const float2 fo = make_float2(d.x * w.x + d.y * w.y, d.y * w.x - d.x * w.y);
+        r[t] = make_float2(fe.x - fo.y, fe.y + fo.x);
+    }
+    warp_fft<E, true>(r, twh, lane);
+    warp_fft_store<E>(r, zb, lane);
+    __syncwarp();
+    for (int i = lane; i < N; i += 32) {
+        const int p = (i & 1) ? (N - 1 - (i >> 1)) : (i >> 1);
+        const float2 z = zb[swz(p >> 1)];
+        float val = (p & 1) ? z.y : z.x;
+        if (sine && (i & 1)) val = -val;
+        emit(i, val);
+    }
+}
+
+// R1 (warp form): rows forward DCT-II, one warp per row.
+template <int E, int NW>
+__global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
+    int m, const float2 *__restrict__ tw_n, const float2 *__restrict__ ek_n,
+    const float *__restrict__ rho_in, unsigned long long *__restrict__ dmap,
+    const float *__restrict__ initial, float fixed_inv, float coef, float inv_area, int zero_map,
+    float *__restrict__ rho_out, float *__restrict__ t1, double *__restrict__ partials,
+    DevState *__restrict__ st, double movable_area) {
+    constexpr int H = 32 * E, N = 2 * H;
+    if (st && st->done) return;
+    extern __shared__ float2 sm[];
+    const AxisTables tb = load_tables<NW, H>(sm, tw_n, ek_n);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float2 *wbase = sm + tables_f2<H>() + warp * 2 * H;
+    float *xm = reinterpret_cast<float *>(wbase);
+    float2 *zb = wbase + H;
+    __shared__ double shr[NW];
+    const int row = blockIdx.x * NW + warp;
+    double ovf = 0.0;
+    const bool from_map = rho_in == nullptr;
+#pragma unroll 8
+    for (int t = 0; t < 2 * E; ++t) {
+        const int i = lane + 32 * t;
+        const size_t idx = (size_t)row * N + i;
+        float v;
+        if (!from_map) {
+            v = rho_in[idx];
+        } else {
+            const unsigned long long q = dmap[idx];
+            if (zero_map) dmap[idx] = 0ull;
+            // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
+            const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q), fixed_inv), initial[idx]);
+            const float o = __fsub_rn(d, coef);
+            ovf += (double)(o > 0.0f ? o : 0.0f);    // src/epotential.rs:274-276
+            v = __fmul_rn(d, inv_area);                // src/epotential.rs:284-285
+            if (rho_out) rho_out[idx] = v;
+        }
+        xm[makhoul_pos(i, N)] = v;
+    }
+    __syncthreads();   // twiddles + staged rows
+    float *out = t1 + (size_t)row * N;
+    warp_dct2_real<E>(xm, zb, tb.twh, tb.tw, tb.ek, lane, [&](int k, float y) { out[k] = y; });
+    if (from_map && partials) {
+        const double b = block_sum(ovf, shr);
+        double vals[1] = {b};
+        if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_OVF], gridDim.x)) {
+            const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
+            if (threadIdx.x == 0) {
+                st->overflow = tot;
+                st->overflow_f = (float)(tot / movable_area);
+                st->ctr[CTR_OVF] = 0;
+            }
+        }
+    }
+}
+
+// C1 (warp form): NW columns per block, one warp per column.  Coalesced tile
+// load, forward DCT-II along x, A and the column's 1/(wu^2+wv^2) kept in shared
+// memory (one division per bin), then for each output kind the weighted inverse
+// along x and a coalesced tile store.
+template <int E, int NW>
+__global__ void __launch_bounds__(NW * 32) k_cols_w(
+    int n, const float2 *__restrict__ tw_m, const float2 *__restrict__ ek_m,
+    const float *__restrict__ wu_g, const float *__restrict__ wv, const float *__restrict__ t1,
+    float *__restrict__ tx, float *__restrict__ ty, float *__restrict__ tp, float scale4,
+    const DevState *__restrict__ st) {
+    constexpr int H = 32 * E, M = 2 * H;
+    constexpr int S = NW + 1;   // tile row stride (odd: conflict-free row-wise access)
+    if (st && st->done) return;
+    extern __shared__ float2 sm[];
+    const AxisTables tb = load_tables<NW, H>(sm, tw_m, ek_m);
+    const float2 *twh = tb.twh;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float *ab = reinterpret_cast<float *>(sm + tables_f2<H>() + warp * 3 * H);   // Makhoul staging, then A
+    float *ib = ab + M;                                                          // 1/(wu^2 + wv^2)
+    float2 *zb = reinterpret_cast<float2 *>(ib + M);                             // FFT staging
+    float *wu = reinterpret_cast<float *>(sm + tables_f2<H>() + NW * 3 * H);
+    float *tile = wu + M;
+    const int j0 = blockIdx.x * NW;
+    for (int k = threadIdx.x; k < M; k += NW * 32) wu[k] = wu_g[k];
+    for (int idx = threadIdx.x; idx < M * NW; idx += NW * 32) {
+        const int i = idx / NW, c = idx - i * NW;
+        tile[i * S + c] = t1[(size_t)i * n + j0 + c];
+    }
+    __syncthreads();
+    const int j = j0 + warp;
+    for (int i = lane; i < M; i += 32) ab[makhoul_pos(i, M)] = tile[i * S + warp];
+    __syncwarp();
+    // forward: results into registers first, then into ab (its Makhoul staging is
+    // consumed by the FFT's register load before the post-processing writes)
+    {
+        float2 r[E];
+        const float2 *ab2 = reinterpret_cast<const float2 *>(ab);
+#pragma unroll
+        for (int k = 0; k < E; ++k) r[k] = ab2[lane + 32 * k];
+        warp_fft<E, false>(r, twh, lane);
+        warp_fft_store<E>(r, zb, lane);
+        __syncwarp();
+        for (int k = lane; k <= H; k += 32) {
+            const float2 zk = zb[swz(k & (H - 1))];
+            float2 zc = zb[swz((H - k) & (H - 1))];
+            zc.y = -zc.y;
+            const float2 ev = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
+            const float2 od = make_float2(0.5f * (zk.y - zc.y), -0.5f * (zk.x - zc.x));
+            const float2 w = k < H ? tb.tw[k] : make_float2(-1.0f, 0.0f);
+            const float2 v = make_float2(ev.x + (w.x * od.x - w.y * od.y), ev.y + (w.x * od.y + w.y * od.x));
+            const float2 e = tb.ek[k];
+            ab[k] = scale4 * (e.x * v.x - e.y * v.y);
+            ib[k] = inv_k2(k, j, wu, wv);
+            if (k > 0 && k < H) {
+                const float2 e2 = tb.ek[M - k];
+                ab[M - k] = scale4 * (e2.x * v.x + e2.y * v.y);
+                ib[M - k] = inv_k2(M - k, j, wu, wv);
+            }
+        }
+        __syncwarp();
+    }
+    const float wvj = wv[j];
+    const int nkinds = tp ? 3 : 2;
+#pragma unroll 1
+    for (int kind = 0; kind < nkinds; ++kind) {
+        // kind 0: field_x  IDXST_x of A * wu / 2k^2   (src/idxst_idct.rs, src/frequencies.rs:52-58)
+        // kind 1: field_y  IDCT_x  of A * wv / 2k^2   (src/idct_idxst.rs, src/frequencies.rs:60-66)
+        // kind 2: potential IDCT_x of A / k^2          (src/idct2.rs)
+        auto xfn = [&](int u) -> float {
+            const float iv = ib[u];
+            float wgt;
+            if (kind == 0) wgt = __fmul_rn(__fmul_rn(wu[u], iv), 0.5f);
+            else if (kind == 1) wgt = __fmul_rn(__fmul_rn(wvj, iv), 0.5f);
+            else wgt = iv;
+            return __fmul_rn(ab[u], wgt);
+        };
+        warp_inv_real<E>(xfn, kind == 0, zb, twh, tb.tw, tb.ek, lane,
+                         [&](int i, float v) { tile[i * S + warp] = v; });
+        __syncthreads();
+        float *out = kind == 0 ? tx : (kind == 1 ? ty : tp);
+        for (int idx = threadIdx.x; idx < M * NW; idx += NW * 32) {
+            const int i = idx / NW, c = idx - i * NW;
+            out[(size_t)i * n + j0 + c] = tile[i * S + c];
+        }
+        __syncthreads();
+    }
+}
+
+// R2 (warp form): rows inverse along y, one warp per (row, output kind).
+template <int E, int NW>
+__global__ void __launch_bounds__(NW * 32) k_rows_inv_w(
+    int m, int nkinds, const float2 *__restrict__ tw_n, const float2 *__restrict__ ek_n,
+    const float *__restrict__ tx, const float *__restrict__ ty, const float *__restrict__ tp,
+    float *__restrict__ fx, float *__restrict__ fy, float *__restrict__ psi,
+    const DevState *__restrict__ st) {
+    constexpr int H = 32 * E, N = 2 * H;
+    if (st && st->done) return;
+    extern __shared__ float2 sm[];
+    const AxisTables tb = load_tables<NW, H>(sm, tw_n, ek_n);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float *xb = reinterpret_cast<float *>(sm + tables_f2<H>() + warp * 2 * H);
+    float2 *zb = sm + tables_f2<H>() + warp * 2 * H + H;
+    __syncthreads();
+    const int task = blockIdx.x * NW + warp;
+    const int row = task / nkinds, kind = task - row * nkinds;
+    // kind 0: field_x = IDCT_y(tx); kind 1: field_y = IDXST_y(ty); kind 2: psi = IDCT_y(tp)
+    const float *in = (kind == 0 ? tx : (kind == 1 ? ty : tp)) + (size_t)row * N;
+    float *out = (kind == 0 ? fx : (kind == 1 ? fy : psi)) + (size_t)row * N;
+#pragma unroll 8
+    for (int t = 0; t < 2 * E; ++t) xb[lane + 32 * t] = in[lane + 32 * t];
+    __syncwarp();
+    warp_inv_real<E>([&](int u) { return xb[u]; }, kind == 1, zb, tb.twh, tb.tw, tb.ek, lane,
+                     [&](int i, float v) { out[i] = v; });
+}
+
 int ilog2(int v) {
     int l = 0;
     while ((1 << l) < v) ++l;
@@ -353,12 +695,38 @@ void spectral_tables(int m, int n, float bin_w, float bin_h, float2 **tw_m, floa
     delete[] h_twm; delete[] h_twn; delete[] h_ekm; delete[] h_ekn; delete[] h_wu; delete[] h_wv;
 }
 
+constexpr int kRowWarps = 4;   // rows per block, warp kernels
+constexpr int kColWarps = 4;   // columns per block, warp kernels
+
+// warp kernels cover N = 64 * E, E = 1..32 (sides 64..2048)
+template <int E>
+static size_t rows_w_smem() { return sizeof(float2) * (size_t)(tables_f2<32 * E>() + kRowWarps * 64 * E); }
+template <int E>
+static size_t cols_w_smem() {
+    return sizeof(float2) * (size_t)(tables_f2<32 * E>() + kColWarps * 96 * E) +
+           sizeof(float) * (size_t)(64 * E) * (kColWarps + 2);
+}
+
+template <int E>
+static cudaError_t prepare_w() {
+    cudaError_t e = cudaFuncSetAttribute(k_rows_dct_w<E, kRowWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_w_smem<E>());
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_inv_w<E, kRowWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_w_smem<E>());
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cols_w<E, kColWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_w_smem<E>());
+    return e;
+}
+
 // Opt the spectral kernels into large dynamic shared memory on the current device.
 cudaError_t spectral_prepare() {
     cudaError_t e = cudaFuncSetAttribute(k_rows_dct<kRowPairs>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_inv<kRowPairs>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cols<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cols<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    if (e == cudaSuccess) e = prepare_w<1>();
+    if (e == cudaSuccess) e = prepare_w<2>();
+    if (e == cudaSuccess) e = prepare_w<4>();
+    if (e == cudaSuccess) e = prepare_w<8>();
+    if (e == cudaSuccess) e = prepare_w<16>();
+    if (e == cudaSuccess) e = prepare_w<32>();
     return e;
 }
 
@@ -367,26 +735,67 @@ size_t spectral_smem_bytes(int m, int n) {
     return a > b ? a : b;
 }
 
+static bool warp_side(int v) { return v >= 64 && v <= 2048; }
+
+template <int E>
+static void rows_dct_w(const SpectralPlan &p, const SpectralArgs &a, bool from_map) {
+    k_rows_dct_w<E, kRowWarps><<<p.m / kRowWarps, kRowWarps * 32, rows_w_smem<E>(), p.stream>>>(
+        p.m, p.tw_n, p.ek_n, a.rho_in, a.dmap, a.initial, a.fixed_inv, a.coef, a.inv_bin_area,
+        a.zero_map ? 1 : 0, a.rho_out, p.t1, from_map ? a.partials : nullptr, a.st, a.movable_area);
+}
+template <int E>
+static void cols_w(const SpectralPlan &p, const SpectralArgs &a, float scale4, float *tp) {
+    k_cols_w<E, kColWarps><<<p.n / kColWarps, kColWarps * 32, cols_w_smem<E>(), p.stream>>>(
+        p.n, p.tw_m, p.ek_m, p.wu, p.wv, p.t1, p.tx, p.ty, tp, scale4, a.st);
+}
+template <int E>
+static void rows_inv_w(const SpectralPlan &p, const SpectralArgs &a, float *tp) {
+    const int nk = tp ? 3 : 2;
+    k_rows_inv_w<E, kRowWarps><<<p.m * nk / kRowWarps, kRowWarps * 32, rows_w_smem<E>(), p.stream>>>(
+        p.m, nk, p.tw_n, p.ek_n, p.tx, p.ty, tp, a.fx, a.fy, a.psi, a.st);
+}
+
+#define ERP_DISPATCH_E(side, FN, ...)           \
+    switch (side) {                             \
+    case 64: FN<1>(__VA_ARGS__); break;         \
+    case 128: FN<2>(__VA_ARGS__); break;        \
+    case 256: FN<4>(__VA_ARGS__); break;        \
+    case 512: FN<8>(__VA_ARGS__); break;        \
+    case 1024: FN<16>(__VA_ARGS__); break;      \
+    default: FN<32>(__VA_ARGS__); break;        \
+    }
+
 void launch_spectral_plan(const SpectralPlan &p, const SpectralArgs &a) {
     const int m = p.m, n = p.n;
     const bool from_map = a.rho_in == nullptr;
     const int rb = m / (2 * kRowPairs);
-    k_rows_dct<kRowPairs><<<rb, kThreads, rows_smem(n, kRowPairs), p.stream>>>(
-        m, n, p.logn, p.tw_n, p.ek_n, a.rho_in, a.dmap, a.initial, a.fixed_inv, a.coef,
-        a.inv_bin_area, a.zero_map ? 1 : 0, a.rho_out, p.t1, from_map ? a.partials : nullptr, a.st,
-        a.movable_area);
+    if (warp_side(n)) {
+        ERP_DISPATCH_E(n, rows_dct_w, p, a, from_map);
+    } else {
+        k_rows_dct<kRowPairs><<<rb, kThreads, rows_smem(n, kRowPairs), p.stream>>>(
+            m, n, p.logn, p.tw_n, p.ek_n, a.rho_in, a.dmap, a.initial, a.fixed_inv, a.coef,
+            a.inv_bin_area, a.zero_map ? 1 : 0, a.rho_out, p.t1, from_map ? a.partials : nullptr, a.st,
+            a.movable_area);
+    }
     const float scale4 = 4.0f / (float)((double)m * (double)n);
     float *tp = a.psi ? p.tp : nullptr;
-    if (col_pairs(m) == 4)
+    if (warp_side(m)) {
+        ERP_DISPATCH_E(m, cols_w, p, a, scale4, tp);
+    } else if (col_pairs(m) == 4) {
         k_cols<4><<<n / 8, kThreads, cols_smem(m, 4), p.stream>>>(m, n, p.logm, p.tw_m, p.ek_m, p.wu,
                                                                   p.wv, p.t1, p.tx, p.ty, tp, scale4,
                                                                   a.st);
-    else
+    } else {
         k_cols<2><<<n / 4, kThreads, cols_smem(m, 2), p.stream>>>(m, n, p.logm, p.tw_m, p.ek_m, p.wu,
                                                                   p.wv, p.t1, p.tx, p.ty, tp, scale4,
                                                                   a.st);
-    k_rows_inv<kRowPairs><<<rb, kThreads, rows_smem(n, kRowPairs), p.stream>>>(
-        m, n, p.logn, p.tw_n, p.ek_n, p.tx, p.ty, tp, a.fx, a.fy, a.psi, a.st);
+    }
+    if (warp_side(n)) {
+        ERP_DISPATCH_E(n, rows_inv_w, p, a, tp);
+    } else {
+        k_rows_inv<kRowPairs><<<rb, kThreads, rows_smem(n, kRowPairs), p.stream>>>(
+            m, n, p.logn, p.tw_n, p.ek_n, p.tx, p.ty, tp, a.fx, a.fy, a.psi, a.st);
+    }
 }
 
 }  // namespace erp

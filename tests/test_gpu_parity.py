@@ -198,6 +198,26 @@ def test_run_retires_at_overflow(R):
     assert it2 == 3 and last2["iteration"] == last["iteration"] + 3
 
 
+@pytest.mark.parametrize("m,n", [(32, 1024), (1024, 32), (2048, 64), (16, 256), (128, 128),
+                                 (1024, 1024)])
+def test_spectral_standalone_shapes(R, O, m, n):
+    """Every transform-size path (warp FFT for 32..1024, shared-memory FFT
+    otherwise) against the FP32 oracle pipeline."""
+    import torch
+    rng = np.random.default_rng(m * 7 + n)
+    rho = (0.5 + rng.random((m, n))).astype(np.float32)
+    bw, bh = 0.9, 1.7
+    fxo, fyo, po = O.poisson(rho, bw, bh, dtype=np.float32)
+    sol = R.SpectralSolver(m, n, bw, bh)
+    r = torch.tensor(rho, device="cuda")
+    out = [torch.empty_like(r) for _ in range(3)]
+    sol.solve(r.data_ptr(), *[t.data_ptr() for t in out])
+    torch.cuda.synchronize()
+    for got, want in zip(out, (fxo, fyo, po)):
+        assert rel_l2(got.cpu().numpy(), want) <= TOL
+    sol.close()
+
+
 def test_spectral_standalone_fp64_error(R, O):
     """Isolated Poisson solve at 512x512 against the FP64 solve (error reported)."""
     import torch
