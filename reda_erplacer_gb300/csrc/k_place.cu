@@ -15,47 +15,57 @@
 namespace erp {
 
 // ============================ wirelength ============================
-// One group of W lanes per net (nets sorted by degree class).  Lane l holds pin
-// l for W >= degree; the >32-pin class loops over pins (LOOP) and recomputes
-// the exponentials in the gradient pass as the reference does
-// (src/hpwl.rs:314-333).  Max-shifted exponentials as in src/hpwl.rs:285-299.
-template <int W, bool LOOP>
-__global__ void __launch_bounds__(kThreads) k_wa(
-    int net_begin, int net_count, int general, const int32_t *__restrict__ net_ptr,
-    const int32_t *__restrict__ slot_cell, const float2 *__restrict__ slot_off,
-    const float *__restrict__ x, const float *__restrict__ y, float2 *__restrict__ slot_grad,
-    float *__restrict__ net_hpwl, const DevState *__restrict__ st, float gamma_arg,
-    float def_min_x, float def_min_y, double *__restrict__ partials, int part_off) {
-    __shared__ double shr[kThreads / 32];
-    if (st->done) return;
-    const float gamma = gamma_arg > 0.f ? gamma_arg : st->gamma;
-    const float inv_gamma = 1.0f / gamma;               // src/hpwl.rs:166
+// One group of W lanes per net (nets sorted by degree class); lane l holds pins
+// l, l + W, ..., l + (P-1) W in registers, so positions are gathered and the
+// four max-shifted exponentials (src/hpwl.rs:285-299) evaluated once per pin
+// and reused for the gradient (the reference recomputes them,
+// src/hpwl.rs:314-333).  Nets with more than W*P pins fall back to a loop that
+// recomputes, like the reference.
+struct WaArgs {
+    const int32_t *net_ptr;
+    const int32_t *slot_cell;
+    const float2 *slot_off;
+    const float *x, *y;
+    float2 *slot_grad;
+    float *net_hpwl;
+    float inv_gamma, def_min_x, def_min_y;
+};
+
+template <int W, int P>
+__device__ __forceinline__ float wa_class(const WaArgs &a, int net_begin, int net_count, int general,
+                                          int cblock, int cgrid) {
     const int gl = threadIdx.x & (W - 1);
     constexpr int GPB = kThreads / W;
+    const float inv_gamma = a.inv_gamma;
     float hp_acc = 0.0f;
-    for (int base = blockIdx.x * GPB; base < net_count; base += gridDim.x * GPB) {
+    for (int base = cblock * GPB; base < net_count; base += cgrid * GPB) {
         const int gid = base + (int)threadIdx.x / W;
         const bool active = gid < net_count;
         const int e = net_begin + gid;
-        const int s0 = active ? net_ptr[e] : 0;
-        const int deg = active ? net_ptr[e + 1] - s0 : 0;
+        const int s0 = active ? a.net_ptr[e] : 0;
+        const int deg = active ? a.net_ptr[e + 1] - s0 : 0;
+        const bool in_regs = deg <= W * P;   // group-uniform
+        float px[P], py[P];
         float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
-        float px = 0.f, py = 0.f;
-        const bool has = !LOOP && gl < deg;
-        if (!LOOP) {
-            if (has) {
-                const int c = slot_cell[s0 + gl];
-                const float2 o = slot_off[s0 + gl];
-                px = x[c] + o.x;                         // src/hpwl.rs:107
-                py = y[c] + o.y;
-                mnx = mxx = px;
-                mny = mxy = py;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const int k = gl + q * W;
+            px[q] = 0.f;
+            py[q] = 0.f;
+            if (in_regs && k < deg) {
+                const int c = a.slot_cell[s0 + k];
+                const float2 o = a.slot_off[s0 + k];
+                px[q] = a.x[c] + o.x;                       // src/hpwl.rs:107
+                py[q] = a.y[c] + o.y;
+                mnx = fminf(mnx, px[q]); mxx = fmaxf(mxx, px[q]);
+                mny = fminf(mny, py[q]); mxy = fmaxf(mxy, py[q]);
             }
-        } else {
+        }
+        if (!in_regs) {
             for (int k = gl; k < deg; k += W) {
-                const int c = slot_cell[s0 + k];
-                const float2 o = slot_off[s0 + k];
-                const float qx = x[c] + o.x, qy = y[c] + o.y;
+                const int c = a.slot_cell[s0 + k];
+                const float2 o = a.slot_off[s0 + k];
+                const float qx = a.x[c] + o.x, qy = a.y[c] + o.y;
                 mnx = fminf(mnx, qx); mxx = fmaxf(mxx, qx);
                 mny = fminf(mny, qy); mxy = fmaxf(mxy, qy);
             }
@@ -68,30 +78,33 @@ __global__ void __launch_bounds__(kThreads) k_wa(
             mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
         }
         if (general) {  // src/hpwl.rs:255-258 initial values
-            mnx = fminf(def_min_x, mnx); mxx = fmaxf(0.0f, mxx);
-            mny = fminf(def_min_y, mny); mxy = fmaxf(0.0f, mxy);
+            mnx = fminf(a.def_min_x, mnx); mxx = fmaxf(0.0f, mxx);
+            mny = fminf(a.def_min_y, mny); mxy = fmaxf(0.0f, mxy);
         }
-        float ex = 0.f, enx = 0.f, ey = 0.f, eny = 0.f;
+        float ex[P], enx[P], ey[P], eny[P];
         float s_xe = 0.f, s_xen = 0.f, s_e = 0.f, s_en = 0.f;
         float s_ye = 0.f, s_yen = 0.f, s_f = 0.f, s_fn = 0.f;
-        if (!LOOP) {
-            if (has) {
-                ex = expf((px - mxx) * inv_gamma);
-                enx = expf((mnx - px) * inv_gamma);
-                ey = expf((py - mxy) * inv_gamma);
-                eny = expf((mny - py) * inv_gamma);
-                s_xe = px * ex; s_xen = px * enx; s_e = ex; s_en = enx;
-                s_ye = py * ey; s_yen = py * eny; s_f = ey; s_fn = eny;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            ex[q] = enx[q] = ey[q] = eny[q] = 0.f;
+            if (in_regs && gl + q * W < deg) {
+                ex[q] = expf((px[q] - mxx) * inv_gamma);
+                enx[q] = expf((mnx - px[q]) * inv_gamma);
+                ey[q] = expf((py[q] - mxy) * inv_gamma);
+                eny[q] = expf((mny - py[q]) * inv_gamma);
+                s_xe += px[q] * ex[q]; s_xen += px[q] * enx[q]; s_e += ex[q]; s_en += enx[q];
+                s_ye += py[q] * ey[q]; s_yen += py[q] * eny[q]; s_f += ey[q]; s_fn += eny[q];
             }
-        } else {
+        }
+        if (!in_regs) {
             for (int k = gl; k < deg; k += W) {
-                const int c = slot_cell[s0 + k];
-                const float2 o = slot_off[s0 + k];
-                const float qx = x[c] + o.x, qy = y[c] + o.y;
-                const float a = expf((qx - mxx) * inv_gamma), b = expf((mnx - qx) * inv_gamma);
-                const float cc = expf((qy - mxy) * inv_gamma), d = expf((mny - qy) * inv_gamma);
-                s_xe += qx * a; s_xen += qx * b; s_e += a; s_en += b;
-                s_ye += qy * cc; s_yen += qy * d; s_f += cc; s_fn += d;
+                const int c = a.slot_cell[s0 + k];
+                const float2 o = a.slot_off[s0 + k];
+                const float qx = a.x[c] + o.x, qy = a.y[c] + o.y;
+                const float e1 = expf((qx - mxx) * inv_gamma), e2 = expf((mnx - qx) * inv_gamma);
+                const float e3 = expf((qy - mxy) * inv_gamma), e4 = expf((mny - qy) * inv_gamma);
+                s_xe += qx * e1; s_xen += qx * e2; s_e += e1; s_en += e2;
+                s_ye += qy * e3; s_yen += qy * e4; s_f += e3; s_fn += e4;
             }
         }
 #pragma unroll
@@ -111,41 +124,75 @@ __global__ void __launch_bounds__(kThreads) k_wa(
         const float b_nx = -inv_gamma / s_en, a_nx = (one - b_nx * s_xen) / s_en;
         const float b_y = inv_gamma / s_f, a_y = (one - b_y * s_ye) / s_f;
         const float b_ny = -inv_gamma / s_fn, a_ny = (one - b_ny * s_yen) / s_fn;
-        if (!LOOP) {
-            if (has)
-                slot_grad[s0 + gl] = make_float2((a_x + b_x * px) * ex - (a_nx + b_nx * px) * enx,
-                                                 (a_y + b_y * py) * ey - (a_ny + b_ny * py) * eny);
-        } else {
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const int k = gl + q * W;
+            if (in_regs && k < deg)
+                a.slot_grad[s0 + k] = make_float2((a_x + b_x * px[q]) * ex[q] - (a_nx + b_nx * px[q]) * enx[q],
+                                                  (a_y + b_y * py[q]) * ey[q] - (a_ny + b_ny * py[q]) * eny[q]);
+        }
+        if (!in_regs) {
             for (int k = gl; k < deg; k += W) {
-                const int c = slot_cell[s0 + k];
-                const float2 o = slot_off[s0 + k];
-                const float qx = x[c] + o.x, qy = y[c] + o.y;
-                const float a = expf((qx - mxx) * inv_gamma), b = expf((mnx - qx) * inv_gamma);
-                const float cc = expf((qy - mxy) * inv_gamma), d = expf((mny - qy) * inv_gamma);
-                slot_grad[s0 + k] = make_float2((a_x + b_x * qx) * a - (a_nx + b_nx * qx) * b,
-                                                (a_y + b_y * qy) * cc - (a_ny + b_ny * qy) * d);
+                const int c = a.slot_cell[s0 + k];
+                const float2 o = a.slot_off[s0 + k];
+                const float qx = a.x[c] + o.x, qy = a.y[c] + o.y;
+                const float e1 = expf((qx - mxx) * inv_gamma), e2 = expf((mnx - qx) * inv_gamma);
+                const float e3 = expf((qy - mxy) * inv_gamma), e4 = expf((mny - qy) * inv_gamma);
+                a.slot_grad[s0 + k] = make_float2((a_x + b_x * qx) * e1 - (a_nx + b_nx * qx) * e2,
+                                                  (a_y + b_y * qy) * e3 - (a_ny + b_ny * qy) * e4);
             }
         }
         if (active && gl == 0) {
             const float hp = (mxx - mnx) + (mxy - mny);   // src/hpwl.rs:302
-            net_hpwl[e] = hp;
+            a.net_hpwl[e] = hp;
             hp_acc += hp;
         }
     }
-    const double b = block_sum((double)hp_acc, shr);
-    if (threadIdx.x == 0) partials[part_off + blockIdx.x] = b;
+    return hp_acc;
 }
 
-// Sum of all per-block HPWL partials (fixed order) -> DevState.hpwl.
-__global__ void k_wl_finalize(const double *__restrict__ partials, int count, DevState *st) {
+// All degree classes in one launch: blocks [cls_block[k], cls_block[k+1]) serve
+// class k.  The block partials of the HPWL total are summed in FP64 by the last
+// block to finish (fixed order, src/hpwl.rs:341-342).
+struct WaClasses {
+    int begin[kNumClasses], count[kNumClasses], general[kNumClasses];
+    int block0[kNumClasses + 1];
+};
+
+__global__ void __launch_bounds__(kThreads) k_wa(WaArgs a, WaClasses cl, float gamma_arg,
+                                                 double *__restrict__ partials, DevState *st) {
     __shared__ double shr[kThreads / 32];
     if (st->done) return;
-    double v = 0.0;
-    for (int k = threadIdx.x; k < count; k += blockDim.x) v += partials[k];
-    v = block_sum(v, shr);
-    if (threadIdx.x == 0) {
-        st->hpwl = v;
-        st->hpwl_f = (float)v;
+    const float gamma = gamma_arg > 0.f ? gamma_arg : st->gamma;
+    a.inv_gamma = 1.0f / gamma;                        // src/hpwl.rs:166
+    int k = 0;
+    while (k + 1 < kNumClasses && (int)blockIdx.x >= cl.block0[k + 1]) ++k;
+    const int cb = blockIdx.x - cl.block0[k], cg = cl.block0[k + 1] - cl.block0[k];
+    float hp;
+    switch (k) {
+    case 0: hp = wa_class<2, 1>(a, cl.begin[0], cl.count[0], cl.general[0], cb, cg); break;
+    case 1: hp = wa_class<4, 1>(a, cl.begin[1], cl.count[1], cl.general[1], cb, cg); break;
+    case 2: hp = wa_class<8, 1>(a, cl.begin[2], cl.count[2], cl.general[2], cb, cg); break;
+    case 3: hp = wa_class<16, 1>(a, cl.begin[3], cl.count[3], cl.general[3], cb, cg); break;
+    case 4: hp = wa_class<32, 1>(a, cl.begin[4], cl.count[4], cl.general[4], cb, cg); break;
+    default: hp = wa_class<32, 4>(a, cl.begin[5], cl.count[5], cl.general[5], cb, cg); break;
+    }
+    const double b = block_sum((double)hp, shr);
+    double vals[1] = {b};
+    if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_HPWL], gridDim.x)) {
+        const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
+        if (threadIdx.x == 0) {
+            st->hpwl = tot;
+            st->hpwl_f = (float)tot;
+            st->ctr[CTR_HPWL] = 0;
+        }
+    }
+}
+
+__global__ void k_wl_zero(DevState *st) {
+    if (threadIdx.x == 0 && !st->done) {
+        st->hpwl = 0.0;
+        st->hpwl_f = 0.0f;
     }
 }
 
@@ -188,9 +235,6 @@ __device__ __forceinline__ float tri_clamped(float x, float s, int k, float bs) 
 // contribution (src/density.rs:195-229), accumulated as rint(v * 2^S) into an
 // int64 map.  Integer sums are order independent, so the privatisation below
 // changes no bit of the result:
-//  * lanes of a warp walk their contributions in lock-step; lanes that hit the
-//    same bin combine their integers first (one atomic per distinct bin per
-//    warp step);
 //  * each block owns a kWin x kWin bin window in shared memory anchored at its
 //    first cell; contributions inside it are accumulated there and flushed with
 //    one global atomic per touched bin, the rest go to global memory directly.
@@ -203,12 +247,9 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
     const float *__restrict__ ch, const float *__restrict__ ratio, int m, int n, float bw,
     float bh, float inv_bw, float inv_bh, float scale, unsigned long long *__restrict__ map,
     const DevState *__restrict__ st) {
-    __shared__ long long sh[kThreads];
     __shared__ unsigned long long win[kWin * kWin];
     __shared__ int s_org[2];
     if (st->done) return;
-    const int lane = threadIdx.x & 31;
-    const int wbase = threadIdx.x & ~31;
     const int per = ((NM + gridDim.x - 1) / gridDim.x + 31) & ~31;
     const int c0 = blockIdx.x * per, c1 = min(c0 + per, NM);
     if (threadIdx.x == 0) {
@@ -244,34 +285,18 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
             ny = max(yh - yl, 0);
         }
         const int cnt = nx * ny;
-        const int maxcnt = __reduce_max_sync(0xffffffffu, (unsigned)cnt);
-        for (int k = 0; k < maxcnt; ++k) {
-            long long c = 0;
-            int key = -1;
-            if (k < cnt) {
-                const int dx = k / ny, dy = k - dx * ny;
-                const int bx = bxl + dx, by = byl + dy;
-                const float px = r * tri_clamped(xi, sxi, bx, bw);
-                const float py = tri_clamped(yi, syi, by, bh);
-                c = __float2ll_rn((px * py) * scale);
-                key = bx * n + by;
-            }
-            const unsigned peers = __match_any_sync(0xffffffffu, key);
-            sh[threadIdx.x] = c;
-            __syncwarp();
-            if (key >= 0 && lane == __ffs(peers) - 1) {
-                long long s = 0;
-                for (unsigned p = peers; p; p &= p - 1) s += sh[wbase + __ffs(p) - 1];
-                if (s) {
-                    const int bx = key / n, by = key - bx * n;
-                    const int wx = bx - wox, wy = by - woy;
-                    if (wx >= 0 && wx < kWin && wy >= 0 && wy < kWin)
-                        atomicAdd(win + wx * kWin + wy, (unsigned long long)s);
-                    else
-                        atomicAdd(map + key, (unsigned long long)s);
-                }
-            }
-            __syncwarp();
+        for (int k = 0; k < cnt; ++k) {
+            const int dx = k / ny, dy = k - dx * ny;
+            const int bx = bxl + dx, by = byl + dy;
+            const float px = r * tri_clamped(xi, sxi, bx, bw);
+            const float py = tri_clamped(yi, syi, by, bh);
+            const long long c = __float2ll_rn((px * py) * scale);
+            if (!c) continue;
+            const int wx = bx - wox, wy = by - woy;
+            if (wx >= 0 && wx < kWin && wy >= 0 && wy < kWin)
+                atomicAdd(win + wx * kWin + wy, (unsigned long long)c);
+            else
+                atomicAdd(map + (size_t)bx * n + by, (unsigned long long)c);
         }
     }
     __syncthreads();
@@ -431,6 +456,44 @@ __global__ void __launch_bounds__(kThreads) k_dw_rescale(int NM, int iter_arg,
 // src/nesterov.rs:143-144, and nothing reads prev_g in between).  The last block
 // applies update_momentum (src/nesterov.rs:148-158) and the adaptive step
 // length (src/nesterov.rs:98-100).
+//
+// Both Nesterov kernels move four cells per thread with 128-bit loads and
+// stores (the per-cell arrays are 256-byte aligned; a scalar tail covers
+// NM % 4).  Each thread's Lipschitz partial over its four cells is FP32 (the
+// products are FP32 in the reference) and the block sums are FP64.
+struct Cell4 {
+    float v[4];
+};
+__device__ __forceinline__ Cell4 ld4(const float *p, int i4) {
+    const float4 t = __ldg(reinterpret_cast<const float4 *>(p) + i4);
+    return Cell4{{t.x, t.y, t.z, t.w}};
+}
+// plain (coherent) load for arrays the same kernel also writes
+__device__ __forceinline__ Cell4 ld4w(const float *p, int i4) {
+    const float4 t = reinterpret_cast<const float4 *>(p)[i4];
+    return Cell4{{t.x, t.y, t.z, t.w}};
+}
+__device__ __forceinline__ void st4(float *p, int i4, const Cell4 &c) {
+    reinterpret_cast<float4 *>(p)[i4] = make_float4(c.v[0], c.v[1], c.v[2], c.v[3]);
+}
+
+__device__ __forceinline__ void nesterov_grad_cell(float wlx, float wly, float dgx_, float dgy_, float w,
+                                                   float h, float np, float x, float y, float px, float py,
+                                                   float &pgx, float &pgy, float dw, float &numf,
+                                                   float &denf) {
+    const float one = 1.0f;
+    const float area = w * h;
+    const float inv_pre = one / fminf(np + dw * area, one);
+    const float gx = (wlx + dw * dgx_) * inv_pre;
+    const float gy = (wly + dw * dgy_) * inv_pre;
+    const float dx = x - px, dy = y - py;
+    const float ddx = gx - pgx, ddy = gy - pgy;
+    pgx = gx;
+    pgy = gy;
+    numf += dx * dx + dy * dy;
+    denf += ddx * ddx + ddy * ddy;
+}
+
 __global__ void __launch_bounds__(kThreads) k_nesterov_grad(
     int NM, int iter_arg, const float *__restrict__ wlgx, const float *__restrict__ wlgy,
     const float *__restrict__ dgx, const float *__restrict__ dgy, const float *__restrict__ w,
@@ -440,29 +503,37 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_grad(
     __shared__ double shr[kThreads / 32];
     if (st->done) return;
     const float dw = st->dw;
-    const float one = 1.0f;
-    double num = 0.0, den = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
-        const float area = w[i] * h[i];
-        const float inv_pre = one / fminf(npins[i] + dw * area, one);
-        const float gx = (wlgx[i] + dw * dgx[i]) * inv_pre;
-        const float gy = (wlgy[i] + dw * dgy[i]) * inv_pre;
-        const float dx = x[i] - px[i], dy = y[i] - py[i];
-        const float ddx = gx - pgx[i], ddy = gy - pgy[i];
+    float numf = 0.0f, denf = 0.0f;
+    const int n4 = NM >> 2;
+    for (int i4 = blockIdx.x * blockDim.x + threadIdx.x; i4 < n4; i4 += gridDim.x * blockDim.x) {
+        const Cell4 a = ld4(wlgx, i4), b = ld4(wlgy, i4), c = ld4(dgx, i4), d = ld4(dgy, i4);
+        const Cell4 ww = ld4(w, i4), hh = ld4(h, i4), np = ld4(npins, i4);
+        const Cell4 xx = ld4(x, i4), yy = ld4(y, i4), qx = ld4(px, i4), qy = ld4(py, i4);
+        Cell4 gx = ld4w(pgx, i4), gy = ld4w(pgy, i4);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            nesterov_grad_cell(a.v[k], b.v[k], c.v[k], d.v[k], ww.v[k], hh.v[k], np.v[k], xx.v[k], yy.v[k],
+                               qx.v[k], qy.v[k], gx.v[k], gy.v[k], dw, numf, denf);
+        st4(pgx, i4, gx);
+        st4(pgy, i4, gy);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (NM & 3)) {   // tail cells
+        const int i = (n4 << 2) + threadIdx.x;
+        float gx = pgx[i], gy = pgy[i];
+        nesterov_grad_cell(wlgx[i], wlgy[i], dgx[i], dgy[i], w[i], h[i], npins[i], x[i], y[i], px[i],
+                           py[i], gx, gy, dw, numf, denf);
         pgx[i] = gx;
         pgy[i] = gy;
-        num += (double)(dx * dx) + (double)(dy * dy);
-        den += (double)(ddx * ddx) + (double)(ddy * ddy);
     }
     double vals[2];
-    vals[0] = block_sum(num, shr);
-    vals[1] = block_sum(den, shr);
+    vals[0] = block_sum((double)numf, shr);
+    vals[1] = block_sum((double)denf, shr);
     if (arrive_last(partials, blockIdx.x, 2, vals, &st->ctr[CTR_LIP], gridDim.x)) {
         const double tn = sum_partials(partials, gridDim.x, 2, 0, shr);
         const double td = sum_partials(partials, gridDim.x, 2, 1, shr);
         if (threadIdx.x == 0) {
             const int it = iter_arg >= 0 ? iter_arg : st->iteration;
-            const float two = one + one, four = two + two;
+            const float one = 1.0f, two = one + one, four = two + two;
             const float a_prev = st->alpha;
             const float na = (one + sqrtf(four * a_prev * a_prev + one)) / two;
             st->beta = (a_prev - one) / na;
@@ -476,24 +547,50 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_grad(
 }
 
 // Lookahead + gradient step + clamp + history (src/nesterov.rs:111-145).
+__device__ __forceinline__ void nesterov_update_cell(float &x, float &y, float &px, float &py, float gx,
+                                                     float gy, float w, float h, float die_w, float die_h,
+                                                     float alpha, float beta) {
+    const float one = 1.0f;
+    const float xo = x, yo = y;
+    const float xh = xo + beta * (xo - px);
+    const float yh = yo + beta * (yo - py);
+    const float hx = die_w - w - one, hy = die_h - h - one;
+    float nx = xh - alpha * gx, ny = yh - alpha * gy;
+    nx = nx < 0.0f ? 0.0f : (nx > hx ? hx : nx);
+    ny = ny < 0.0f ? 0.0f : (ny > hy ? hy : ny);
+    px = xo;
+    py = yo;
+    x = nx;
+    y = ny;
+}
+
 __global__ void __launch_bounds__(kThreads) k_nesterov_update(
     int NM, const float *__restrict__ w, const float *__restrict__ h, float die_w, float die_h,
     float *__restrict__ x, float *__restrict__ y, float *__restrict__ px, float *__restrict__ py,
     const float *__restrict__ gx, const float *__restrict__ gy, const DevState *__restrict__ st) {
     if (st->done) return;
-    const float alpha = st->alpha, beta = st->beta, one = 1.0f;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
-        const float xo = x[i], yo = y[i];
-        const float xh = xo + beta * (xo - px[i]);
-        const float yh = yo + beta * (yo - py[i]);
-        const float hx = die_w - w[i] - one, hy = die_h - h[i] - one;
-        float nx = xh - alpha * gx[i], ny = yh - alpha * gy[i];
-        nx = nx < 0.0f ? 0.0f : (nx > hx ? hx : nx);
-        ny = ny < 0.0f ? 0.0f : (ny > hy ? hy : ny);
-        px[i] = xo;
-        py[i] = yo;
-        x[i] = nx;
-        y[i] = ny;
+    const float alpha = st->alpha, beta = st->beta;
+    const int n4 = NM >> 2;
+    for (int i4 = blockIdx.x * blockDim.x + threadIdx.x; i4 < n4; i4 += gridDim.x * blockDim.x) {
+        Cell4 xx = ld4w(x, i4), yy = ld4w(y, i4), qx = ld4w(px, i4), qy = ld4w(py, i4);
+        const Cell4 a = ld4(gx, i4), b = ld4(gy, i4), ww = ld4(w, i4), hh = ld4(h, i4);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            nesterov_update_cell(xx.v[k], yy.v[k], qx.v[k], qy.v[k], a.v[k], b.v[k], ww.v[k], hh.v[k], die_w,
+                                 die_h, alpha, beta);
+        st4(x, i4, xx);
+        st4(y, i4, yy);
+        st4(px, i4, qx);
+        st4(py, i4, qy);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (NM & 3)) {
+        const int i = (n4 << 2) + threadIdx.x;
+        float xi = x[i], yi = y[i], pxi = px[i], pyi = py[i];
+        nesterov_update_cell(xi, yi, pxi, pyi, gx[i], gy[i], w[i], h[i], die_w, die_h, alpha, beta);
+        x[i] = xi;
+        y[i] = yi;
+        px[i] = pxi;
+        py[i] = pyi;
     }
 }
 
@@ -552,30 +649,36 @@ static int grid_for(int work, int cap = 152 * 8) {
 }
 
 void launch_wirelength(Ctx &c, float gamma_arg) {
-    int off = 0;
-    const float def_min_x = c.die_w + 1.0f, def_min_y = c.die_h + 1.0f;
+    WaArgs a;
+    a.net_ptr = c.net_ptr;
+    a.slot_cell = c.slot_cell;
+    a.slot_off = c.slot_off;
+    a.x = c.x;
+    a.y = c.y;
+    a.slot_grad = c.slot_grad;
+    a.net_hpwl = c.net_hpwl;
+    a.inv_gamma = 0.f;
+    a.def_min_x = c.die_w + 1.0f;
+    a.def_min_y = c.die_h + 1.0f;
+    WaClasses cl;
+    int blocks = 0;
     for (int k = 0; k < kNumClasses; ++k) {
         const NetClass &nc = c.cls[k];
-        if (nc.count == 0) continue;
-        const int groups_per_block = kThreads / nc.width;
-        int grid = (nc.count + groups_per_block - 1) / groups_per_block;
-        if (grid > 1024) grid = 1024;
-#define ERP_WA(WW, LL)                                                                                      \
-    k_wa<WW, LL><<<grid, kThreads, 0, c.stream>>>(nc.begin, nc.count, nc.general, c.net_ptr, c.slot_cell,   \
-                                                  c.slot_off, c.x, c.y, c.slot_grad, c.net_hpwl, c.st,      \
-                                                  gamma_arg, def_min_x, def_min_y, c.partials, off)
-        switch (k) {
-        case 0: ERP_WA(2, false); break;
-        case 1: ERP_WA(4, false); break;
-        case 2: ERP_WA(8, false); break;
-        case 3: ERP_WA(16, false); break;
-        case 4: ERP_WA(32, false); break;
-        default: ERP_WA(32, true); break;
-        }
-#undef ERP_WA
-        off += grid;
+        cl.begin[k] = nc.begin;
+        cl.count[k] = nc.count;
+        cl.general[k] = nc.general;
+        cl.block0[k] = blocks;
+        const int gpb = kThreads / nc.width;
+        int g = (nc.count + gpb - 1) / gpb;
+        if (g > 1024) g = 1024;
+        blocks += g;
     }
-    k_wl_finalize<<<1, kThreads, 0, c.stream>>>(c.partials, off, c.st);
+    cl.block0[kNumClasses] = blocks;
+    if (blocks == 0) {   // no nets: the total is zero
+        k_wl_zero<<<1, 32, 0, c.stream>>>(c.st);
+        return;
+    }
+    k_wa<<<blocks, kThreads, 0, c.stream>>>(a, cl, gamma_arg, c.partials, c.st);
 }
 
 void launch_wl_gather(Ctx &c) {
@@ -637,10 +740,11 @@ void launch_nesterov(Ctx &c, int iter_arg) {
     const int g = grid_for(c.NM);
     k_dw_rescale<<<g, kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx, c.dgy,
                                                c.partials, c.st);
-    k_nesterov_grad<<<g, kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx, c.dgy, c.w,
+    const int g4 = grid_for((c.NM + 3) / 4);
+    k_nesterov_grad<<<g4, kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx, c.dgy, c.w,
                                                   c.h, c.npins, c.x, c.y, c.prev_x, c.prev_y,
                                                   c.prev_gx, c.prev_gy, c.partials, c.st);
-    k_nesterov_update<<<g, kThreads, 0, c.stream>>>(c.NM, c.w, c.h, c.die_w, c.die_h, c.x, c.y,
+    k_nesterov_update<<<g4, kThreads, 0, c.stream>>>(c.NM, c.w, c.h, c.die_w, c.die_h, c.x, c.y,
                                                     c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.st);
 }
 
