@@ -163,6 +163,52 @@ def cpu_sample(d, cfg, iters, literal):
     return iters / dt, dt
 
 
+def batch_section(args, device):
+    """Batched workload: 64 instances (cells log-uniform 2k-200k, nets 1.05x,
+    macros 0-16, bins = pow2 nearest sqrt(cells)/2 in 64..1024), each to 600
+    iterations or overflow <= 0.10.  Jobs/hour of the batched graph (all
+    instances in one CUDA graph) against running the same jobs one at a time
+    through erp_run; both include context creation."""
+    import torch
+    import reda_erplacer_gb300 as R
+    mix = R.workload_batch(count=args.batch_count)
+    designs = [d for d, _ in mix]
+    bins = [b for _, b in mix]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bt = R.Batch(designs, bins, 1.0, start_mode=1, device=device)
+    t_bcreate = time.perf_counter() - t0
+    its, lasts = bt.run(args.batch_iters, stop_overflow=0.10)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    bt.close()
+    seq_lat = []
+    t0 = time.perf_counter()
+    seq_its = []
+    t_screate = 0.0
+    for d, b in mix:
+        t1 = time.perf_counter()
+        pl = R.Placement(d, b, 1.0, start_mode=1, device=device)
+        t_screate += time.perf_counter() - t1
+        it, last = pl.run(args.batch_iters, stop_overflow=0.10)
+        pl.close()
+        seq_its.append(it)
+        seq_lat.append(time.perf_counter() - t1)
+    t_seq = time.perf_counter() - t0
+    K = len(mix)
+    return {
+        "instances": K, "cells": [int(d.num_movable) for d in designs],
+        "bins": [int(b[0]) for b in bins], "max_iterations": args.batch_iters, "stop_overflow": 0.10,
+        "iterations_total": int(sum(its)), "retired_at_overflow": int(sum(1 for l in lasts if l["overflow"] <= 0.10)),
+        "batched_s": t_batch, "sequential_s": t_seq,
+        "batched_create_s": t_bcreate, "sequential_create_s": t_screate,
+        "jobs_per_hour_batched": K / t_batch * 3600.0, "jobs_per_hour_sequential": K / t_seq * 3600.0,
+        "speedup": t_seq / t_batch, "same_iterations": its == seq_its,
+        "sequential_latency_p50_s": float(statistics.median(seq_lat)),
+        "spectral": "FP32 (the BF16 split spectral form is not built)",
+    }
+
+
 def run_reference(args):
     world, rank, local = dist_setup()
     if rank != 0:
@@ -282,6 +328,8 @@ def run_ours(args):
                      "traffic": traffic, "alg_bytes": alg[dom], "ms": stages[dom]},
         "stages": per_stage,
     }
+    if args.batch_count > 0:
+        line["batched"] = batch_section(args, local)
     if rank == 0 and world == 1 and not args.no_cpu:
         v, dt = cpu_sample(d, cfg, args.cpu_iters, literal=False)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
@@ -304,6 +352,8 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true", help="timed steps only (for profiler runs)")
+    ap.add_argument("--batch-count", type=int, default=64, help="instances of the batched section (0: skip)")
+    ap.add_argument("--batch-iters", type=int, default=600)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -202,6 +202,28 @@ erp_status erp_get_array(erp_ctx *ctx, erp_array which, void *dst, size_t bytes)
 /* Block until the context's stream is idle. */
 erp_status erp_synchronize(erp_ctx *ctx);
 
+/* ---- batched instances ----
+ * Many designs advance together (the reference drives one design from its CLI
+ * loop, src/main.rs:78-90; here that loop runs for a whole table of designs).
+ * One CUDA graph holds one branch per instance -- each branch is that
+ * instance's whole Placement::step -- so one graph launch moves every unfinished
+ * instance by one iteration and independent instances overlap on the GPU.  An
+ * instance retires on the device once its overflow <= stop_overflow or its
+ * iteration budget is spent; its kernels then return at entry. */
+typedef struct erp_batch erp_batch;
+erp_status erp_batch_create(const erp_design *designs, const erp_params *params, int32_t count,
+                            erp_batch **out);
+/* Run every instance for up to max_iterations more steps (stop_overflow <= 0:
+ * never early).  iterations[i] and last[i] (either may be NULL) receive each
+ * instance's step count and final step record. */
+erp_status erp_batch_run(erp_batch *b, int32_t max_iterations, float stop_overflow,
+                         int32_t *iterations, erp_step_stats *last);
+/* The context of instance i (owned by the batch: do not destroy it). */
+erp_ctx *erp_batch_context(erp_batch *b, int32_t i);
+int32_t erp_batch_size(const erp_batch *b);
+const char *erp_batch_last_error(const erp_batch *b);
+void erp_batch_destroy(erp_batch *b);
+
 /* ---- profiling (the reference's time_it phases, src/utils.rs:106-124) ----
  * Times each stage of one step in isolation: `reps` launches, each preceded by
  * an L2 flush (a 256 MiB device write, untimed), bracketed by CUDA events on

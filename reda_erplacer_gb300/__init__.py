@@ -4,10 +4,10 @@ include/erplacer.h.  All compute runs in liberplacer_gb300.so; importing this
 package fails if the library has not been built (no fallback)."""
 from . import lib
 from .lib import ErpError
-from .design import Design, synth, workload_small, workload_large, bins_for_cells
-from .placement import Placement, SpectralSolver
+from .design import Design, synth, workload_small, workload_large, workload_batch, bins_for_cells
+from .placement import Batch, Placement, SpectralSolver
 
 lib.load()
 
-__all__ = ["Design", "synth", "workload_small", "workload_large", "bins_for_cells", "Placement",
-           "SpectralSolver", "ErpError"]
+__all__ = ["Design", "synth", "workload_small", "workload_large", "workload_batch", "bins_for_cells",
+           "Placement", "Batch", "SpectralSolver", "ErpError"]

@@ -6,6 +6,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -489,11 +491,9 @@ extern "C" erp_status erp_should_stop(erp_ctx *ctx, int32_t *stop) {
     return s;
 }
 
-static erp_status ensure_graph(Ctx &c) {
-    if (c.graph_ready) return ERP_OK;
-    cudaGraph_t g;
-    CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-    // Placement::step order (src/placement.rs:180-228)
+namespace erp {
+// Placement::step order (src/placement.rs:180-228)
+void enqueue_step_kernels(Ctx &c) {
     launch_wirelength(c, -1.0f);
     launch_wl_gather(c);
     launch_density_scatter(c);
@@ -501,21 +501,34 @@ static erp_status ensure_graph(Ctx &c) {
     launch_force(c);
     launch_nesterov(c, -1);
     launch_scheduler(c, 0, 0.f, 0.f);
+}
+}  // namespace erp
+
+static int count_kernel_nodes(cudaGraph_t g) {
+    size_t nn = 0;
+    cudaGraphGetNodes(g, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+    int k = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+    }
+    return k;
+}
+
+static erp_status ensure_graph(Ctx &c) {
+    if (c.graph_ready) return ERP_OK;
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step_kernels(c);
     cudaError_t e = cudaStreamEndCapture(c.stream, &g);
     if (e != cudaSuccess) {
         c.err = std::string("graph capture: ") + cudaGetErrorString(e);
         cudaGetLastError();
         return ERP_ECUDA;
     }
-    size_t nn = 0;
-    cudaGraphGetNodes(g, nullptr, &nn);
-    std::vector<cudaGraphNode_t> nodes(nn);
-    if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
-    c.graph_kernels = 0;
-    for (auto nd : nodes) {
-        cudaGraphNodeType t;
-        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) c.graph_kernels++;
-    }
+    c.graph_kernels = count_kernel_nodes(g);
     e = cudaGraphInstantiate(&c.graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {
@@ -783,6 +796,254 @@ extern "C" erp_status erp_profile_stages(erp_ctx *ctx, int32_t reps, float *ms_o
         if (err != cudaSuccess) { c.err = cudaGetErrorString(err); rc = ERP_ECUDA; }
     }
     return rc;
+}
+
+// ---------------------------------------------------------------------------
+// batched instances: one graph, one branch per instance
+struct erp_batch {
+    std::vector<erp_ctx *> ctx;
+    cudaStream_t master = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    bool graph_ready = false;
+    int graph_kernels = 0;
+    DevState **d_states = nullptr;   // device array of the instances' state pointers
+    int32_t *d_done = nullptr;
+    int32_t *h_done = nullptr;       // pinned
+    int device = 0;
+    std::string err;
+};
+
+static erp_status batch_fail(erp_batch *b, erp_status s, const std::string &msg) {
+    b->err = msg;
+    return s;
+}
+
+extern "C" erp_status erp_batch_create(const erp_design *designs, const erp_params *params,
+                                       int32_t count, erp_batch **out) {
+    g_create_err.clear();
+    if (!out || !designs || count < 1) {
+        g_create_err = "invalid batch arguments";
+        return ERP_EINVAL;
+    }
+    *out = nullptr;
+    erp_batch *b = new (std::nothrow) erp_batch();
+    if (!b) return ERP_ENOMEM;
+    erp_status s = ERP_OK;
+    // Instances are independent: their host-side set-up (validation, net
+    // classes, pin renumbering, uploads) runs on several host threads.
+    std::vector<erp_ctx *> made(count, nullptr);
+    std::vector<erp_status> st(count, ERP_OK);
+    std::vector<std::string> msg(count);
+    std::atomic<int> next(0);
+    auto worker = [&]() {
+        for (int i = next++; i < count; i = next++) {
+            erp_params p;
+            memset(&p, 0, sizeof p);
+            if (params) p = params[i];
+            p.stream = nullptr;   // every instance gets its own stream (its graph branch)
+            st[i] = erp_create(designs + i, &p, &made[i]);
+            if (st[i] != ERP_OK) msg[i] = g_create_err;
+        }
+    };
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = std::max(1u, std::min(nt ? nt : 1u, std::min(16u, (unsigned)count)));
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto &t : pool) t.join();
+    for (int i = 0; i < count; ++i) {
+        if (made[i]) b->ctx.push_back(made[i]);
+        if (st[i] != ERP_OK && s == ERP_OK) {
+            s = st[i];
+            g_create_err = "instance " + std::to_string(i) + ": " + msg[i];
+        }
+    }
+    if (s == ERP_OK) {
+        b->device = b->ctx[0]->c.device;
+        for (auto *c : b->ctx)
+            if (c->c.device != b->device) {
+                s = ERP_EINVAL;
+                g_create_err = "all instances of a batch must use the same device";
+            }
+    }
+    if (s == ERP_OK) {
+        cudaSetDevice(b->device);
+        std::vector<DevState *> sts;
+        for (auto *c : b->ctx) sts.push_back(c->c.st);
+        bool ok = cudaStreamCreateWithFlags(&b->master, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaMalloc(&b->d_states, sizeof(DevState *) * count) == cudaSuccess &&
+                  cudaMalloc(&b->d_done, sizeof(int32_t) * count * 2) == cudaSuccess &&
+                  cudaMallocHost(&b->h_done, sizeof(int32_t) * count * 2) == cudaSuccess &&
+                  cudaMemcpy(b->d_states, sts.data(), sizeof(DevState *) * count, cudaMemcpyHostToDevice) == cudaSuccess;
+        if (!ok) {
+            s = ERP_ENOMEM;
+            g_create_err = "batch allocation failed";
+        }
+    }
+    if (s != ERP_OK) {
+        erp_batch_destroy(b);
+        return s;
+    }
+    *out = b;
+    return ERP_OK;
+}
+
+// (Re)capture the batch graph over the instances whose active flag is set.
+static erp_status batch_graph(erp_batch *b, const std::vector<char> &active) {
+    if (b->graph_ready) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph_ready = false;
+    }
+    cudaEvent_t fork;
+    if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess)
+        return batch_fail(b, ERP_ECUDA, "cudaEventCreate failed");
+    std::vector<cudaEvent_t> joins(b->ctx.size());
+    for (auto &e : joins) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    cudaGraph_t g;
+    cudaError_t e = cudaStreamBeginCapture(b->master, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaEventRecord(fork, b->master);
+        for (size_t i = 0; i < b->ctx.size(); ++i) {
+            if (!active[i]) continue;
+            Ctx &c = b->ctx[i]->c;
+            cudaStreamWaitEvent(c.stream, fork, 0);
+            enqueue_step_kernels(c);
+            cudaEventRecord(joins[i], c.stream);
+            cudaStreamWaitEvent(b->master, joins[i], 0);
+        }
+        e = cudaStreamEndCapture(b->master, &g);
+    }
+    if (e == cudaSuccess) {
+        b->graph_kernels = count_kernel_nodes(g);
+        e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+    }
+    cudaEventDestroy(fork);
+    for (auto &j : joins) cudaEventDestroy(j);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return batch_fail(b, ERP_ECUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+    }
+    b->graph_ready = true;
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_batch_run(erp_batch *b, int32_t max_iterations, float stop_overflow,
+                                    int32_t *iterations, erp_step_stats *last) {
+    if (!b || max_iterations < 0) return ERP_EINVAL;
+    b->err.clear();
+    if (cudaSetDevice(b->device) != cudaSuccess) return batch_fail(b, ERP_ECUDA, "cudaSetDevice failed");
+    const int K = (int)b->ctx.size();
+    std::vector<int> start(K);
+    for (int i = 0; i < K; ++i) {
+        Ctx &c = b->ctx[i]->c;
+        erp_status s = pull_state(c);
+        if (s != ERP_OK) return batch_fail(b, s, "instance " + std::to_string(i) + ": " + c.err);
+        start[i] = c.h_st->iteration;
+        // arm: retire at overflow or after max_iterations more steps
+        c.h_st->stop_overflow = stop_overflow > 0 ? stop_overflow : 0.0f;
+        c.h_st->stop_iter = start[i] + max_iterations;
+        c.h_st->done = max_iterations == 0 ? 1 : 0;
+        if (c.map_dirty) {
+            cudaMemsetAsync(c.dmap, 0, sizeof(unsigned long long) * (size_t)c.m * c.n, c.stream);
+            c.map_dirty = false;
+        }
+        if (cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream) != cudaSuccess ||
+            cudaStreamSynchronize(c.stream) != cudaSuccess)
+            return batch_fail(b, ERP_ECUDA, "arming instance failed");
+    }
+    // Launch the graph in chunks; the retire flags of chunk k are read while
+    // chunk k+1 runs (double-buffered), and when instances have retired the
+    // graph is captured again over the remaining ones.
+    std::vector<char> active(K, max_iterations > 0 ? 1 : 0);
+    int n_active = max_iterations > 0 ? K : 0;
+    erp_status s = n_active ? batch_graph(b, active) : ERP_OK;
+    if (s != ERP_OK) return s;
+    const int chunk = 16;
+    int launched = 0;
+    cudaEvent_t ev[2];
+    cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+    int pending = -1;
+    erp_status rs = ERP_OK;
+    while (n_active > 0 && launched < max_iterations) {
+        const int k = std::min(chunk, max_iterations - launched);
+        for (int i = 0; i < k && rs == ERP_OK; ++i)
+            if (cudaGraphLaunch(b->graph, b->master) != cudaSuccess)
+                rs = batch_fail(b, ERP_ECUDA, "batch graph launch failed");
+        if (rs != ERP_OK) break;
+        launched += k;
+        const int buf = (launched / chunk) & 1;
+        launch_gather_done(b->d_states, K, b->d_done + buf * K, b->master);
+        cudaMemcpyAsync(b->h_done + buf * K, b->d_done + buf * K, sizeof(int32_t) * K, cudaMemcpyDeviceToHost,
+                        b->master);
+        cudaEventRecord(ev[buf], b->master);
+        if (pending >= 0) {
+            if (cudaEventSynchronize(ev[pending]) != cudaSuccess) {
+                rs = batch_fail(b, ERP_ECUDA, std::string("batch run: ") + cudaGetErrorString(cudaGetLastError()));
+                break;
+            }
+            int now = 0;
+            for (int i = 0; i < K; ++i) now += active[i] && !b->h_done[pending * K + i];
+            if (now < n_active) {   // some retired: drop their branches
+                for (int i = 0; i < K; ++i)
+                    if (b->h_done[pending * K + i]) active[i] = 0;
+                n_active = now;
+                if (n_active > 0) {
+                    cudaStreamSynchronize(b->master);
+                    rs = batch_graph(b, active);
+                    if (rs != ERP_OK) break;
+                }
+            }
+        }
+        pending = buf;
+    }
+    cudaStreamSynchronize(b->master);
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    if (rs != ERP_OK) return rs;
+    erp_status rc = ERP_OK;
+    for (int i = 0; i < K; ++i) {
+        Ctx &c = b->ctx[i]->c;
+        erp_status si = pull_state(c);
+        if (iterations) iterations[i] = c.h_st->iteration - start[i];
+        if (last) last[i] = c.h_st->last;
+        // disarm
+        c.h_st->stop_overflow = 0.0f;
+        c.h_st->stop_iter = 0;
+        c.h_st->done = 0;
+        cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream);
+        cudaStreamSynchronize(c.stream);
+        if (si != ERP_OK && rc == ERP_OK) {
+            rc = si;
+            b->err = "instance " + std::to_string(i) + ": " + c.err;
+        }
+    }
+    return rc;
+}
+
+extern "C" erp_ctx *erp_batch_context(erp_batch *b, int32_t i) {
+    if (!b || i < 0 || i >= (int)b->ctx.size()) return nullptr;
+    return b->ctx[i];
+}
+
+extern "C" int32_t erp_batch_size(const erp_batch *b) { return b ? (int32_t)b->ctx.size() : 0; }
+
+extern "C" const char *erp_batch_last_error(const erp_batch *b) {
+    return b ? b->err.c_str() : g_create_err.c_str();
+}
+
+extern "C" void erp_batch_destroy(erp_batch *b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->master) cudaStreamSynchronize(b->master);
+    if (b->graph_ready) cudaGraphExecDestroy(b->graph);
+    for (auto *c : b->ctx) erp_destroy(c);
+    if (b->master) cudaStreamDestroy(b->master);
+    if (b->d_states) cudaFree(b->d_states);
+    if (b->d_done) cudaFree(b->d_done);
+    if (b->h_done) cudaFreeHost(b->h_done);
+    delete b;
 }
 
 // ---------------------------------------------------------------------------

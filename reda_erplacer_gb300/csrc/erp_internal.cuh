@@ -40,6 +40,7 @@ struct DevState {
     int32_t done;          // set once overflow <= stop threshold: kernels become no-ops
     int32_t status;        // bit 0: non-finite value seen
     float stop_overflow;   // <= 0: never stop
+    int32_t stop_iter;     // > 0: retire once iteration reaches it
     int32_t last_iter;     // iteration index of the last completed step
     erp_step_stats last;   // stats of the last completed step
     // last-block counters of the deterministic reductions
@@ -119,6 +120,10 @@ void launch_energy(Ctx &c);
 // optimiser + scheduler (src/nesterov.rs, src/scheduler.rs)
 void launch_nesterov(Ctx &c, int iter_arg);                // iter_arg < 0: read DevState.iteration
 void launch_scheduler(Ctx &c, int use_args, float hpwl, float overflow);
+// One whole Placement::step on the context's stream (the graph's content).
+void enqueue_step_kernels(Ctx &c);
+// Gather the retire flags of several contexts into out[i] (device pointers).
+void launch_gather_done(DevState *const *states, int count, int32_t *out, cudaStream_t s);
 
 // spectral engine for the standalone solve
 struct SpectralPlan {

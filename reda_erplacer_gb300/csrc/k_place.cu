@@ -640,6 +640,16 @@ __global__ void k_scheduler(int use_args, float hpwl_arg, float ovf_arg, DevStat
         st->done = 1;
     }
     if (st->stop_overflow > 0.0f && ovf <= st->stop_overflow) st->done = 1;
+    if (st->stop_iter > 0 && st->iteration >= st->stop_iter) st->done = 1;
+}
+
+__global__ void k_gather_done(DevState *const *states, int count, int32_t *out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        out[i] = states[i]->done;
+}
+
+void launch_gather_done(DevState *const *states, int count, int32_t *out, cudaStream_t s) {
+    k_gather_done<<<(count + 255) / 256, 256, 0, s>>>(states, count, out);
 }
 
 // ============================ launchers ============================

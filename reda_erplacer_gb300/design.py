@@ -116,6 +116,22 @@ def workload_large(seed=2):
         dict(bins=(1024, 1024), target_density=1.0, iterations=1000)
 
 
+def workload_batch(count=64, seed=4000, min_cells=2000, max_cells=200000):
+    """Instance mix of the batched workload: cells log-uniform in [min, max], nets
+    1.05 x cells, macros uniform 0-16, bin grid = power of two nearest
+    sqrt(cells)/2 clamped to 64..1024; each instance its own seed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        cells = int(round(np.exp(rng.uniform(np.log(min_cells), np.log(max_cells)))))
+        macros = int(rng.integers(0, 17))
+        d = synth(cells, int(round(1.05 * cells)), num_io=max(4, cells // 250), num_macros=macros,
+                  macro_area_frac=0.015, utilization=0.65, seed=seed + 1 + i)
+        b = bins_for_cells(cells)
+        out.append((d, (b, b)))
+    return out
+
+
 def bins_for_cells(num_cells):
     """Power of two nearest sqrt(cells)/2, clamped to 64..1024 (batched-instance rule)."""
     t = np.sqrt(num_cells) / 2.0

@@ -100,6 +100,12 @@ EXPORTS = {
     "erp_spectral_destroy": (None, [C.c_void_p]),
     "erp_spectral_solve_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_void_p,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "erp_batch_create": (C.c_int, [C.POINTER(Design), C.POINTER(Params), C.c_int32, C.POINTER(C.c_void_p)]),
+    "erp_batch_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_float, i32p, C.POINTER(StepStats)]),
+    "erp_batch_context": (C.c_void_p, [C.c_void_p, C.c_int32]),
+    "erp_batch_size": (C.c_int32, [C.c_void_p]),
+    "erp_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "erp_batch_destroy": (None, [C.c_void_p]),
     "erp_synth_create": (C.c_int, [C.POINTER(SynthParams), C.POINTER(C.c_void_p)]),
     "erp_synth_design": (C.c_int, [C.c_void_p, C.POINTER(Design)]),
     "erp_synth_destroy": (None, [C.c_void_p]),

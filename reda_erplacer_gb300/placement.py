@@ -158,6 +158,53 @@ class Placement:
         return out
 
 
+class Batch:
+    """Many designs advanced together by one CUDA graph (one branch per design);
+    see erp_batch_* in include/erplacer.h."""
+
+    def __init__(self, designs, num_bins, target_density=1.0, start_mode=L.START_CENTER, device=0):
+        self.lib = L.load()
+        K = len(designs)
+        self._structs = [d.to_struct() for d in designs]
+        darr = (L.Design * K)(*self._structs)
+        bins = num_bins if isinstance(num_bins[0], (tuple, list)) else [num_bins] * K
+        parr = (L.Params * K)(*[L.Params(int(b[0]), int(b[1]), float(target_density), int(start_mode),
+                                         L.PREC_FP32, int(device), None, 0) for b in bins])
+        h = C.c_void_p()
+        st = self.lib.erp_batch_create(darr, parr, K, C.byref(h))
+        L.check(st, None)
+        self.h = h
+        self.K = K
+        self.designs = designs
+
+    def run(self, max_iterations, stop_overflow=0.0):
+        it = (C.c_int32 * self.K)()
+        last = (L.StepStats * self.K)()
+        st = self.lib.erp_batch_run(self.h, int(max_iterations), float(stop_overflow), it, last)
+        if st != L.OK:
+            raise L.ErpError(st, self.lib.erp_batch_last_error(self.h).decode())
+        return [int(v) for v in it], [s.as_dict() for s in last]
+
+    def positions(self, i):
+        ctx = self.lib.erp_batch_context(self.h, int(i))
+        N = int(self.designs[i].num_nodes)
+        x = np.empty(N, np.float32)
+        y = np.empty(N, np.float32)
+        L.check(self.lib.erp_get_positions(ctx, x.ctypes.data_as(L.f32p), y.ctypes.data_as(L.f32p)), ctx)
+        return x, y
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.erp_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class SpectralSolver:
     """Standalone Poisson solve (src/epotential.rs:284-343) on device pointers."""
 
