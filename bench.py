@@ -209,6 +209,42 @@ def batch_section(args, device):
     }
 
 
+def serve_section(args, device):
+    """Serving workload: an open-loop stream of jobs (cells log-uniform 5k-500k,
+    each its own seed) with Poisson arrivals at 80 % of the capacity measured by
+    a batched pilot run; admission under a 150 GB HBM budget, retire at overflow
+    <= 0.10 or 600 iterations.  p50/p99 completion latency and jobs/hour of the
+    continuous-batching server, and of the same stream served one job at a
+    time."""
+    import numpy as np
+    import reda_erplacer_gb300 as R
+    from reda_erplacer_gb300.serving import Server, run_stream
+    mix = R.workload_batch(count=args.serve_jobs, seed=9000, min_cells=5000, max_cells=500000)
+    pilot = mix[: min(32, len(mix))]
+    bt = R.Batch([d for d, _ in pilot], [b for _, b in pilot], 1.0, start_mode=1, device=device)
+    t0 = time.perf_counter()
+    bt.run(args.batch_iters, stop_overflow=0.10)
+    cap = len(pilot) / (time.perf_counter() - t0)
+    bt.close()
+    rate = 0.8 * cap
+    rng = np.random.default_rng(17)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(mix)))
+    out = {"jobs": len(mix), "capacity_jobs_per_s": cap, "arrival_rate_jobs_per_s": rate,
+           "hbm_budget_gb": 150.0, "max_iterations": args.batch_iters, "stop_overflow": 0.10}
+    for name, max_active in (("continuous_batching", 64), ("one_at_a_time", 1)):
+        sv = Server(max_active=max_active, hbm_budget_gb=150.0, max_iterations=args.batch_iters,
+                    stop_overflow=0.10, chunk=8, device=device)
+        res = run_stream(sv, mix, arrivals)
+        sv.close()
+        lat = np.array([r["latency_s"] for r in res])
+        span = max(r["finish_s"] for r in res) - min(r["submit_s"] for r in res)
+        out[name] = {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+                     "jobs_per_hour": len(res) / span * 3600.0, "makespan_s": span,
+                     "failed": int(sum(1 for r in res if r["status"] != 0)),
+                     "retired_at_overflow": int(sum(1 for r in res if r["last"]["overflow"] <= 0.10))}
+    return out
+
+
 def run_reference(args):
     world, rank, local = dist_setup()
     if rank != 0:
@@ -330,6 +366,8 @@ def run_ours(args):
     }
     if args.batch_count > 0:
         line["batched"] = batch_section(args, local)
+    if args.serve:
+        line["serving"] = serve_section(args, local)
     if rank == 0 and world == 1 and not args.no_cpu:
         v, dt = cpu_sample(d, cfg, args.cpu_iters, literal=False)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
@@ -354,6 +392,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="timed steps only (for profiler runs)")
     ap.add_argument("--batch-count", type=int, default=64, help="instances of the batched section (0: skip)")
     ap.add_argument("--batch-iters", type=int, default=600)
+    ap.add_argument("--serve", action="store_true", help="also run the serving stream")
+    ap.add_argument("--serve-jobs", type=int, default=200)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

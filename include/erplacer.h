@@ -224,6 +224,50 @@ int32_t erp_batch_size(const erp_batch *b);
 const char *erp_batch_last_error(const erp_batch *b);
 void erp_batch_destroy(erp_batch *b);
 
+/* ---- serving: continuous batching of placement jobs ----
+ * Jobs are submitted as they arrive and wait in a FIFO queue.  Each
+ * erp_server_pump round admits queued jobs while their device footprint fits
+ * the HBM budget (and the active-job cap), runs `chunk` iterations of every
+ * active job in one batched graph (re-captured when the active set changes),
+ * and retires jobs whose overflow <= stop_overflow or whose iteration budget is
+ * spent, freeing their memory for the next admissions.  Times are seconds on
+ * the server's steady clock. */
+typedef struct erp_server_params {
+    int32_t device;
+    int32_t max_active;         /* jobs on the GPU at once (1: one job at a time) */
+    int64_t hbm_budget_bytes;   /* admission budget for the jobs' device memory */
+    int32_t max_iterations;     /* per job */
+    float stop_overflow;        /* retire threshold (<= 0: run max_iterations) */
+    int32_t chunk;              /* iterations per scheduling round */
+    int32_t keep_positions;     /* 1: keep each retired job's final positions */
+} erp_server_params;
+
+typedef struct erp_job_result {
+    int64_t job_id;
+    int32_t status;             /* erp_status of the job */
+    int32_t iterations;
+    erp_step_stats last;
+    double submit_s, admit_s, finish_s;
+    int64_t footprint_bytes;
+} erp_job_result;
+
+typedef struct erp_server erp_server;
+erp_status erp_server_create(const erp_server_params *p, erp_server **out);
+/* Queue a job (the design's arrays are copied).  params may be NULL. */
+erp_status erp_server_submit(erp_server *s, int64_t job_id, const erp_design *design,
+                             const erp_params *params);
+/* One scheduling round; reports the active and queued job counts. */
+erp_status erp_server_pump(erp_server *s, int32_t *active, int32_t *queued);
+/* Move up to `cap` finished jobs into out[]; *count receives how many. */
+erp_status erp_server_poll(erp_server *s, erp_job_result *out, int32_t cap, int32_t *count);
+/* Final positions of a retired job (keep_positions = 1). */
+erp_status erp_server_positions(erp_server *s, int64_t job_id, float *x, float *y);
+double erp_server_now(const erp_server *s);
+const char *erp_server_last_error(const erp_server *s);
+void erp_server_destroy(erp_server *s);
+/* Device bytes a context for this design would allocate. */
+erp_status erp_estimate_footprint(const erp_design *design, const erp_params *params, int64_t *bytes);
+
 /* ---- profiling (the reference's time_it phases, src/utils.rs:106-124) ----
  * Times each stage of one step in isolation: `reps` launches, each preceded by
  * an L2 flush (a 256 MiB device write, untimed), bracketed by CUDA events on

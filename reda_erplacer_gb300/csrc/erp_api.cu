@@ -7,6 +7,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <memory>
 #include <thread>
 #include <string>
 #include <vector>
@@ -54,9 +56,12 @@ namespace {
 
 bool pow2_ok(int v) { return v >= 16 && v <= 4096 && (v & (v - 1)) == 0; }
 
+// Stream-ordered allocations on the context's stream: creating or destroying a
+// context never synchronises the device, so jobs can be admitted and retired
+// while other contexts' work runs.
 template <typename T>
-cudaError_t dalloc(T **p, size_t count) {
-    return cudaMalloc((void **)p, sizeof(T) * (count ? count : 1));
+cudaError_t dalloc(T **p, size_t count, cudaStream_t s) {
+    return cudaMallocAsync((void **)p, sizeof(T) * (count ? count : 1), s);
 }
 
 cudaError_t upload(void *dst, const void *src, size_t bytes, cudaStream_t s) {
@@ -146,8 +151,11 @@ void free_ctx(Ctx &c) {
                     c.slot_grad, c.net_ptr, c.net_hpwl, c.cell_slot_ptr, c.cell_slots, c.dmap,
                     c.initial, c.rho, c.t1, c.tx, c.ty, c.tp, c.fx, c.fy, c.psi, c.tw_m, c.tw_n,
                     c.ek_m, c.ek_n, c.wu, c.wv, c.partials, c.st};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
+    for (void *p : ptrs) {   // stream-ordered, on the stream they were allocated on
+        if (!p) continue;
+        if (c.stream) cudaFreeAsync(p, c.stream);
+        else cudaFree(p);
+    }
     if (c.h_st) cudaFreeHost(c.h_st);
     if (c.graph_ready) cudaGraphExecDestroy(c.graph);
     if (c.own_stream && c.stream) cudaStreamDestroy(c.stream);
@@ -323,20 +331,21 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     const size_t mn = (size_t)c.m * c.n;
     float **cellarr[] = {&c.x, &c.y, &c.w, &c.h, &c.npins, &c.cw, &c.ch, &c.offx, &c.offy, &c.ratio,
                          &c.wlgx, &c.wlgy, &c.dgx, &c.dgy, &c.prev_x, &c.prev_y, &c.prev_gx, &c.prev_gy};
-    for (float **a : cellarr) CK(dalloc(a, (size_t)N + 4));
-    CK(dalloc(&c.slot_cell, P));
-    CK(dalloc(&c.slot_off, P));
-    CK(dalloc(&c.slot_grad, P));
-    CK(dalloc(&c.net_ptr, (size_t)E + 1));
-    CK(dalloc(&c.net_hpwl, E));
-    CK(dalloc(&c.cell_slot_ptr, (size_t)NM + 1));
-    CK(dalloc(&c.cell_slots, hcell_slots.size()));
-    CK(dalloc(&c.dmap, mn));
+    cudaStream_t s0 = c.stream;
+    for (float **a : cellarr) CK(dalloc(a, (size_t)N + 4, s0));
+    CK(dalloc(&c.slot_cell, P, s0));
+    CK(dalloc(&c.slot_off, P, s0));
+    CK(dalloc(&c.slot_grad, P, s0));
+    CK(dalloc(&c.net_ptr, (size_t)E + 1, s0));
+    CK(dalloc(&c.net_hpwl, E, s0));
+    CK(dalloc(&c.cell_slot_ptr, (size_t)NM + 1, s0));
+    CK(dalloc(&c.cell_slots, hcell_slots.size(), s0));
+    CK(dalloc(&c.dmap, mn, s0));
     float **maps[] = {&c.initial, &c.rho, &c.t1, &c.tx, &c.ty, &c.tp, &c.fx, &c.fy, &c.psi};
-    for (float **a : maps) CK(dalloc(a, mn));
-    CK(dalloc(&c.partials, kMaxPartials));
+    for (float **a : maps) CK(dalloc(a, mn, s0));
+    CK(dalloc(&c.partials, kMaxPartials, s0));
     c.max_partials = kMaxPartials;
-    CK(dalloc(&c.st, 1));
+    CK(dalloc(&c.st, 1, s0));
     CK(cudaMallocHost((void **)&c.h_st, sizeof(DevState)));
     spectral_tables(c.m, c.n, c.bin_w, c.bin_h, &c.tw_m, &c.tw_n, &c.ek_m, &c.ek_n, &c.wu, &c.wv, c.stream);
     CK(cudaGetLastError());
@@ -1044,6 +1053,332 @@ extern "C" void erp_batch_destroy(erp_batch *b) {
     if (b->d_done) cudaFree(b->d_done);
     if (b->h_done) cudaFreeHost(b->h_done);
     delete b;
+}
+
+// ---------------------------------------------------------------------------
+// serving: continuous batching
+extern "C" erp_status erp_estimate_footprint(const erp_design *d, const erp_params *pp, int64_t *bytes) {
+    if (!d || !bytes) return ERP_EINVAL;
+    int m = pp && pp->num_bins_x ? pp->num_bins_x : 512, n = pp && pp->num_bins_y ? pp->num_bins_y : 512;
+    const int64_t N = d->num_nodes, NM = d->num_movable, P = d->num_pins, E = d->num_nets;
+    const int64_t mn = (int64_t)m * n;
+    int64_t movable_pins = 0;
+    if (d->inst_pin_ptr) movable_pins = d->inst_pin_ptr[NM];
+    auto al = [](int64_t v) { return (v + 511) & ~int64_t(511); };   // allocation granularity
+    int64_t b = 18 * al(4 * (N + 4));
+    b += al(4 * P) + 2 * al(8 * P) + al(4 * (E + 1)) + al(4 * E) + al(4 * (NM + 1)) + al(4 * movable_pins);
+    b += al(8 * mn) + 9 * al(4 * mn) + al(8 * (int64_t)kMaxPartials) + al(sizeof(DevState));
+    b += al(8 * (m / 2)) + al(8 * (n / 2)) + al(8 * m) + al(8 * n) + al(4 * m) + al(4 * n);
+    *bytes = b;
+    return ERP_OK;
+}
+
+namespace {
+struct OwnedDesign {
+    std::vector<float> x, y, w, h, npins, pox, poy;
+    std::vector<int32_t> pin_inst, net_ptr, net_pins, inst_ptr, inst_pins;
+    erp_design d;
+    explicit OwnedDesign(const erp_design &s) {
+        d = s;
+        const size_t N = s.num_nodes, P = s.num_pins, E = s.num_nets;
+        auto cpf = [](std::vector<float> &v, const float *p, size_t k) { v.assign(p, p + (p ? k : 0)); };
+        auto cpi = [](std::vector<int32_t> &v, const int32_t *p, size_t k) { v.assign(p, p + (p ? k : 0)); };
+        cpf(x, s.x, N); cpf(y, s.y, N); cpf(w, s.w, N); cpf(h, s.h, N); cpf(npins, s.num_pins_f, N);
+        cpf(pox, s.pin_ox, P); cpf(poy, s.pin_oy, P);
+        cpi(pin_inst, s.pin_inst, P);
+        cpi(net_ptr, s.net_ptr, E + 1);
+        cpi(net_pins, s.net_pins, s.net_ptr ? (size_t)s.net_ptr[E] : 0);
+        cpi(inst_ptr, s.inst_pin_ptr, N + 1);
+        cpi(inst_pins, s.inst_pins, s.inst_pin_ptr ? (size_t)s.inst_pin_ptr[N] : 0);
+        d.x = x.data(); d.y = y.data(); d.w = w.data(); d.h = h.data(); d.num_pins_f = npins.data();
+        d.pin_ox = pox.data(); d.pin_oy = poy.data(); d.pin_inst = pin_inst.data();
+        d.net_ptr = net_ptr.data(); d.net_pins = net_pins.data();
+        d.inst_pin_ptr = inst_ptr.data(); d.inst_pins = inst_pins.data();
+    }
+};
+struct Job {
+    int64_t id = 0;
+    std::unique_ptr<OwnedDesign> des;
+    erp_params prm;
+    double submit = 0, admit = 0;
+    int64_t footprint = 0;
+    erp_ctx *ctx = nullptr;
+    int start_iter = 0;
+};
+}  // namespace
+
+struct erp_server {
+    erp_server_params p;
+    std::vector<std::unique_ptr<Job>> queue;   // FIFO (front = index qhead)
+    size_t qhead = 0;
+    std::vector<std::unique_ptr<Job>> active;
+    std::vector<erp_job_result> finished;
+    std::vector<std::pair<int64_t, std::pair<std::vector<float>, std::vector<float>>>> pos;
+    int64_t used = 0;
+    cudaStream_t master = nullptr;
+    std::vector<cudaEvent_t> job_ev;   // one per slot
+    cudaEvent_t round_ev[2] = {nullptr, nullptr};
+    bool round_pending[2] = {false, false};
+    std::vector<int64_t> round_ids[2];
+    uint64_t round_seq[2] = {0, 0};
+    uint64_t rounds_launched = 0;
+    std::vector<std::pair<uint64_t, std::unique_ptr<Job>>> grave;   // (last round that references it, job)
+    int round = 0;
+    DevState **d_states = nullptr;       // [2][max_active]
+    int32_t *d_done = nullptr, *h_done = nullptr;
+    std::chrono::steady_clock::time_point t0;
+    std::string err;
+    double now() const {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
+
+extern "C" erp_status erp_server_create(const erp_server_params *p, erp_server **out) {
+    g_create_err.clear();
+    if (!p || !out || p->max_active < 1 || p->hbm_budget_bytes <= 0 || p->max_iterations < 1 || p->chunk < 1) {
+        g_create_err = "invalid server parameters";
+        return ERP_EINVAL;
+    }
+    erp_status s = check_device(p->device, g_create_err);
+    if (s != ERP_OK) return s;
+    erp_server *sv = new (std::nothrow) erp_server();
+    if (!sv) return ERP_ENOMEM;
+    sv->p = *p;
+    sv->t0 = std::chrono::steady_clock::now();
+    const int K = p->max_active;
+    bool ok = cudaStreamCreateWithFlags(&sv->master, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaMalloc(&sv->d_states, sizeof(DevState *) * 2 * K) == cudaSuccess &&
+              cudaMalloc(&sv->d_done, sizeof(int32_t) * 2 * K) == cudaSuccess &&
+              cudaMallocHost(&sv->h_done, sizeof(int32_t) * 2 * K) == cudaSuccess &&
+              cudaEventCreateWithFlags(&sv->round_ev[0], cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&sv->round_ev[1], cudaEventDisableTiming) == cudaSuccess;
+    sv->job_ev.resize(K, nullptr);
+    for (int i = 0; ok && i < K; ++i)
+        ok = cudaEventCreateWithFlags(&sv->job_ev[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        erp_server_destroy(sv);
+        g_create_err = "server allocation failed";
+        return ERP_ENOMEM;
+    }
+    *out = sv;
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_server_submit(erp_server *sv, int64_t job_id, const erp_design *d,
+                                        const erp_params *prm) {
+    if (!sv || !d) return ERP_EINVAL;
+    auto j = std::make_unique<Job>();
+    j->id = job_id;
+    j->des = std::make_unique<OwnedDesign>(*d);
+    memset(&j->prm, 0, sizeof j->prm);
+    if (prm) j->prm = *prm;
+    j->prm.stream = nullptr;
+    j->prm.device = sv->p.device;
+    erp_estimate_footprint(&j->des->d, &j->prm, &j->footprint);
+    j->submit = sv->now();
+    sv->queue.push_back(std::move(j));
+    return ERP_OK;
+}
+
+// Record a finished job's result (stats, optionally positions); the context
+// itself is destroyed later by server_bury.
+static void server_record(erp_server *sv, Job &j, erp_status st) {
+    erp_job_result r;
+    memset(&r, 0, sizeof r);
+    r.job_id = j.id;
+    r.status = st;
+    r.submit_s = j.submit;
+    r.admit_s = j.admit;
+    r.footprint_bytes = j.footprint;
+    if (j.ctx) {
+        Ctx &c = j.ctx->c;
+        erp_status ps = pull_state(c);
+        if (st == ERP_OK) r.status = ps;
+        r.iterations = c.h_st->iteration - j.start_iter;
+        r.last = c.h_st->last;
+        if (sv->p.keep_positions) {
+            std::vector<float> x(c.N), y(c.N);
+            cudaMemcpyAsync(x.data(), c.x, sizeof(float) * c.N, cudaMemcpyDeviceToHost, c.stream);
+            cudaMemcpyAsync(y.data(), c.y, sizeof(float) * c.N, cudaMemcpyDeviceToHost, c.stream);
+            cudaStreamSynchronize(c.stream);
+            sv->pos.emplace_back(j.id, std::make_pair(std::move(x), std::move(y)));
+        }
+    }
+    r.finish_s = sv->now();
+    sv->finished.push_back(r);
+}
+
+// One scheduling round.  Every active job launches its own captured step graph
+// `chunk` times on its own stream (so admissions and retirements never touch
+// the other jobs' work), then the round's retire flags are gathered behind an
+// event.  A pump launches round r first and only then reads the flags of round
+// r-1, so the GPU always has queued work while the host retires and admits.
+// A job retired from round r-1's flags still ran round r (its kernels return
+// at entry once retired) and round r's flag gather reads its state, so its
+// context is destroyed only after round r has completed (the graveyard).
+static erp_status server_launch_round(erp_server *sv, int buf) {
+    const int K = (int)sv->active.size();
+    std::vector<DevState *> sts(K);
+    sv->round_ids[buf].clear();
+    for (int i = 0; i < K; ++i) {
+        Ctx &c = sv->active[i]->ctx->c;
+        erp_status s = ensure_graph(c);
+        if (s != ERP_OK) {
+            sv->err = c.err;
+            return s;
+        }
+        for (int k = 0; k < sv->p.chunk; ++k)
+            if (cudaGraphLaunch(c.graph, c.stream) != cudaSuccess) {
+                sv->err = "job graph launch failed";
+                return ERP_ECUDA;
+            }
+        cudaEventRecord(sv->job_ev[i], c.stream);
+        cudaStreamWaitEvent(sv->master, sv->job_ev[i], 0);
+        sts[i] = c.st;
+        sv->round_ids[buf].push_back(sv->active[i]->id);
+    }
+    const int off = buf * sv->p.max_active;
+    cudaMemcpyAsync(sv->d_states + off, sts.data(), sizeof(DevState *) * K, cudaMemcpyHostToDevice, sv->master);
+    launch_gather_done(sv->d_states + off, K, sv->d_done + off, sv->master);
+    cudaMemcpyAsync(sv->h_done + off, sv->d_done + off, sizeof(int32_t) * K, cudaMemcpyDeviceToHost, sv->master);
+    cudaEventRecord(sv->round_ev[buf], sv->master);
+    sv->round_pending[buf] = true;
+    sv->round_seq[buf] = ++sv->rounds_launched;
+    return ERP_OK;
+}
+
+static void server_bury(erp_server *sv, uint64_t completed_round) {
+    std::vector<std::pair<uint64_t, std::unique_ptr<Job>>> keep;
+    for (auto &g : sv->grave) {
+        if (g.first <= completed_round) {
+            erp_destroy(g.second->ctx);
+            g.second->ctx = nullptr;
+            sv->used -= g.second->footprint;
+        } else {
+            keep.push_back(std::move(g));
+        }
+    }
+    sv->grave.swap(keep);
+}
+
+extern "C" erp_status erp_server_pump(erp_server *sv, int32_t *active_out, int32_t *queued_out) {
+    if (!sv) return ERP_EINVAL;
+    sv->err.clear();
+    if (cudaSetDevice(sv->p.device) != cudaSuccess) return ERP_ECUDA;
+    const int cur = sv->round, prev = sv->round ^ 1;
+    // 1. launch this round for the active jobs
+    const bool launched = !sv->active.empty();
+    if (launched) {
+        erp_status s = server_launch_round(sv, cur);
+        if (s != ERP_OK) return s;
+    }
+    // 2. read the previous round's flags; retire (record results) the done jobs
+    if (sv->round_pending[prev]) {
+        if (cudaEventSynchronize(sv->round_ev[prev]) != cudaSuccess) {
+            sv->err = std::string("server round: ") + cudaGetErrorString(cudaGetLastError());
+            return ERP_ECUDA;
+        }
+        sv->round_pending[prev] = false;
+        server_bury(sv, sv->round_seq[prev]);   // contexts retired before round prev
+        const auto &ids = sv->round_ids[prev];
+        std::vector<int64_t> done;
+        for (size_t i = 0; i < ids.size(); ++i)
+            if (sv->h_done[prev * sv->p.max_active + i]) done.push_back(ids[i]);
+        if (!done.empty()) {
+            std::vector<std::unique_ptr<Job>> keep;
+            const uint64_t last_ref = launched ? sv->round_seq[cur] : sv->round_seq[prev];
+            for (auto &j : sv->active) {
+                if (std::find(done.begin(), done.end(), j->id) != done.end()) {
+                    server_record(sv, *j, ERP_OK);
+                    sv->grave.emplace_back(last_ref, std::move(j));
+                } else {
+                    keep.push_back(std::move(j));
+                }
+            }
+            sv->active.swap(keep);
+        }
+    }
+    if (!launched && !sv->round_pending[cur] && !sv->round_pending[prev])
+        server_bury(sv, sv->rounds_launched);   // idle: everything launched has completed
+    // 3. admission: FIFO while the job fits the budget and a slot is free
+    while (sv->qhead < sv->queue.size() && (int)sv->active.size() < sv->p.max_active) {
+        Job &j = *sv->queue[sv->qhead];
+        if (j.footprint > sv->p.hbm_budget_bytes) {   // can never fit
+            std::unique_ptr<Job> jp = std::move(sv->queue[sv->qhead++]);
+            server_record(sv, *jp, ERP_ENOMEM);
+            continue;
+        }
+        if (sv->used + j.footprint > sv->p.hbm_budget_bytes) break;
+        std::unique_ptr<Job> jp = std::move(sv->queue[sv->qhead++]);
+        erp_status s = erp_create(&jp->des->d, &jp->prm, &jp->ctx);
+        jp->admit = sv->now();
+        if (s != ERP_OK) {
+            jp->ctx = nullptr;
+            server_record(sv, *jp, s);
+            continue;
+        }
+        Ctx &c = jp->ctx->c;
+        c.h_st->stop_overflow = sv->p.stop_overflow > 0 ? sv->p.stop_overflow : 0.0f;
+        c.h_st->stop_iter = sv->p.max_iterations;
+        c.h_st->done = 0;
+        cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream);
+        jp->start_iter = 0;
+        sv->used += jp->footprint;
+        jp->des.reset();   // the context holds its own copy
+        sv->active.push_back(std::move(jp));
+    }
+    if (sv->qhead > 1024 && sv->qhead * 2 > sv->queue.size()) {   // compact the FIFO
+        sv->queue.erase(sv->queue.begin(), sv->queue.begin() + sv->qhead);
+        sv->qhead = 0;
+    }
+    if (launched) sv->round ^= 1;
+    if (active_out) *active_out = (int32_t)sv->active.size();
+    if (queued_out) *queued_out = (int32_t)(sv->queue.size() - sv->qhead);
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_server_poll(erp_server *sv, erp_job_result *out, int32_t cap, int32_t *count) {
+    if (!sv || !count || (cap > 0 && !out)) return ERP_EINVAL;
+    const int k = std::min<int>(cap, (int)sv->finished.size());
+    for (int i = 0; i < k; ++i) out[i] = sv->finished[i];
+    sv->finished.erase(sv->finished.begin(), sv->finished.begin() + k);
+    *count = k;
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_server_positions(erp_server *sv, int64_t job_id, float *x, float *y) {
+    if (!sv || !x || !y) return ERP_EINVAL;
+    for (auto &e : sv->pos)
+        if (e.first == job_id) {
+            std::copy(e.second.first.begin(), e.second.first.end(), x);
+            std::copy(e.second.second.begin(), e.second.second.end(), y);
+            return ERP_OK;
+        }
+    sv->err = "no kept positions for this job";
+    return ERP_EINVAL;
+}
+
+extern "C" double erp_server_now(const erp_server *sv) { return sv ? sv->now() : 0.0; }
+
+extern "C" const char *erp_server_last_error(const erp_server *sv) { return sv ? sv->err.c_str() : g_create_err.c_str(); }
+
+extern "C" void erp_server_destroy(erp_server *sv) {
+    if (!sv) return;
+    cudaSetDevice(sv->p.device);
+    if (sv->master) cudaStreamSynchronize(sv->master);
+    for (auto &j : sv->active)
+        if (j->ctx) erp_destroy(j->ctx);
+    for (auto &g : sv->grave)
+        if (g.second->ctx) erp_destroy(g.second->ctx);
+    for (auto e : sv->job_ev)
+        if (e) cudaEventDestroy(e);
+    for (auto e : sv->round_ev)
+        if (e) cudaEventDestroy(e);
+    if (sv->master) cudaStreamDestroy(sv->master);
+    if (sv->d_states) cudaFree(sv->d_states);
+    if (sv->d_done) cudaFree(sv->d_done);
+    if (sv->h_done) cudaFreeHost(sv->h_done);
+    delete sv;
 }
 
 // ---------------------------------------------------------------------------

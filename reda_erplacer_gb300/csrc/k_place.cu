@@ -717,16 +717,16 @@ void launch_initial_density(Ctx &c, const float *, const float *, const float *,
             hcy[i] = (l + hh) / 2.0f;
         }
         float *dcx, *dcy;
-        cudaMalloc(&dcx, sizeof(float) * c.m);
-        cudaMalloc(&dcy, sizeof(float) * c.n);
+        cudaMallocAsync(&dcx, sizeof(float) * c.m, c.stream);
+        cudaMallocAsync(&dcy, sizeof(float) * c.n, c.stream);
         cudaMemcpyAsync(dcx, hcx, sizeof(float) * c.m, cudaMemcpyHostToDevice, c.stream);
         cudaMemcpyAsync(dcy, hcy, sizeof(float) * c.n, cudaMemcpyHostToDevice, c.stream);
         k_initial_density<<<count < 4096 ? count : 4096, kThreads, 0, c.stream>>>(
             c.NM, count, c.x, c.y, c.w, c.h, dcx, dcy, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw, c.inv_bh,
             ldexpf(1.0f, c.shift0), c.dmap);
         cudaStreamSynchronize(c.stream);
-        cudaFree(dcx);
-        cudaFree(dcy);
+        cudaFreeAsync(dcx, c.stream);
+        cudaFreeAsync(dcy, c.stream);
         delete[] hcx;
         delete[] hcy;
     }

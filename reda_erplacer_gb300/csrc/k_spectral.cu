@@ -679,12 +679,12 @@ void spectral_tables(int m, int n, float bin_w, float bin_h, float2 **tw_m, floa
     const float wv_div = bin_w / bin_h;
     const float tpn = (float)(2.0 * 3.14159265358979323846) / (float)n;
     for (int j = 0; j < n; ++j) h_wv[j] = ((float)j * tpn) * wv_div;
-    cudaMalloc(tw_m, sizeof(float2) * (m / 2));
-    cudaMalloc(tw_n, sizeof(float2) * (n / 2));
-    cudaMalloc(ek_m, sizeof(float2) * m);
-    cudaMalloc(ek_n, sizeof(float2) * n);
-    cudaMalloc(wu, sizeof(float) * m);
-    cudaMalloc(wv, sizeof(float) * n);
+    cudaMallocAsync(tw_m, sizeof(float2) * (m / 2), s);
+    cudaMallocAsync(tw_n, sizeof(float2) * (n / 2), s);
+    cudaMallocAsync(ek_m, sizeof(float2) * m, s);
+    cudaMallocAsync(ek_n, sizeof(float2) * n, s);
+    cudaMallocAsync(wu, sizeof(float) * m, s);
+    cudaMallocAsync(wv, sizeof(float) * n, s);
     cudaMemcpyAsync(*tw_m, h_twm, sizeof(float2) * (m / 2), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(*tw_n, h_twn, sizeof(float2) * (n / 2), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(*ek_m, h_ekm, sizeof(float2) * m, cudaMemcpyHostToDevice, s);

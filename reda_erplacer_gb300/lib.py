@@ -72,7 +72,33 @@ class SynthParams(C.Structure):
                 ("min_sites", C.c_int32), ("max_sites", C.c_int32), ("jitter_frac", C.c_float)]
 
 
+class ServerParams(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_active", C.c_int32), ("hbm_budget_bytes", C.c_int64),
+                ("max_iterations", C.c_int32), ("stop_overflow", C.c_float), ("chunk", C.c_int32),
+                ("keep_positions", C.c_int32)]
+
+
+class JobResult(C.Structure):
+    _fields_ = [("job_id", C.c_int64), ("status", C.c_int32), ("iterations", C.c_int32),
+                ("last", StepStats), ("submit_s", C.c_double), ("admit_s", C.c_double),
+                ("finish_s", C.c_double), ("footprint_bytes", C.c_int64)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "last"}
+        d["last"] = self.last.as_dict()
+        return d
+
+
 EXPORTS = {
+    "erp_server_create": (C.c_int, [C.POINTER(ServerParams), C.POINTER(C.c_void_p)]),
+    "erp_server_submit": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(Design), C.POINTER(Params)]),
+    "erp_server_pump": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "erp_server_poll": (C.c_int, [C.c_void_p, C.POINTER(JobResult), C.c_int32, C.POINTER(C.c_int32)]),
+    "erp_server_positions": (C.c_int, [C.c_void_p, C.c_int64, f32p, f32p]),
+    "erp_server_now": (C.c_double, [C.c_void_p]),
+    "erp_server_last_error": (C.c_char_p, [C.c_void_p]),
+    "erp_server_destroy": (None, [C.c_void_p]),
+    "erp_estimate_footprint": (C.c_int, [C.POINTER(Design), C.POINTER(Params), C.POINTER(C.c_int64)]),
     "erp_status_string": (C.c_char_p, [C.c_int]),
     "erp_last_error": (C.c_char_p, [C.c_void_p]),
     "erp_abi_version": (C.c_int32, []),
