@@ -27,7 +27,7 @@ CU_SOURCES = {
     "erp_noalloc.cu": [],
 }
 CPP_SOURCES = ["synth.cpp"]
-HEADERS = ["erp_internal.cuh", "reduce.cuh"]
+HEADERS = ["erp_internal.cuh", "reduce.cuh", "bulk_copy.cuh"]
 
 
 def _deps():

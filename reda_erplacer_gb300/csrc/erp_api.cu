@@ -429,6 +429,10 @@ extern "C" void erp_destroy(erp_ctx *ctx) {
 static erp_status pull_state(Ctx &c) {
     CK(cudaMemcpyAsync(c.h_st, c.st, sizeof(DevState), cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
+    if (c.h_st->status & kStatusWaitTimeout) {
+        c.err = "a bulk copy into shared memory did not complete within the wait limit";
+        return ERP_ETIMEDOUT;
+    }
     if (c.h_st->status & 1) {
         c.err = "non-finite HPWL, overflow or step length";
         return ERP_ENAN;

@@ -38,7 +38,7 @@ struct DevState {
     float hpwl_f, overflow_f;
     // step bookkeeping
     int32_t done;          // set once overflow <= stop threshold: kernels become no-ops
-    int32_t status;        // bit 0: non-finite value seen
+    int32_t status;        // bit 0: non-finite value seen; bit 1: a bounded wait ran out
     float stop_overflow;   // <= 0: never stop
     int32_t stop_iter;     // > 0: retire once iteration reaches it
     int32_t last_iter;     // iteration index of the last completed step
@@ -46,6 +46,8 @@ struct DevState {
     // last-block counters of the deterministic reductions
     uint32_t ctr[8];
 };
+
+constexpr int32_t kStatusWaitTimeout = 2;   // DevState::status bit 1
 
 enum Counter { CTR_HPWL = 0, CTR_OVF = 1, CTR_ABS = 2, CTR_LIP = 3, CTR_ENERGY = 4 };
 

@@ -22,6 +22,7 @@
 // radix-2 decimation-in-frequency pass in shared memory (natural order in,
 // bit-reversed order out), twiddles from FP64-computed tables.
 #include "erp_internal.cuh"
+#include "bulk_copy.cuh"
 #include "reduce.cuh"
 
 namespace erp {
@@ -72,7 +73,7 @@ __global__ void __launch_bounds__(kThreads) k_rows_dct(
     float *__restrict__ rho_out, float *__restrict__ t1, double *__restrict__ partials,
     DevState *__restrict__ st, double movable_area) {
     if (st && st->done) return;
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     float2 *tw = sm;
     float2 *buf = sm + (n >> 1);
     __shared__ double shr[kThreads / 32];
@@ -145,7 +146,7 @@ __global__ void __launch_bounds__(kThreads) k_cols(
     const DevState *__restrict__ st) {
     if (st && st->done) return;
     constexpr int CB = 2 * CP;
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     float2 *tw = sm;
     float2 *buf = sm + (m >> 1);
     float *A = reinterpret_cast<float *>(buf + CP * m);
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(kThreads) k_rows_inv(
     float *__restrict__ fx, float *__restrict__ fy, float *__restrict__ psi,
     const DevState *__restrict__ st) {
     if (st && st->done) return;
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     float2 *tw = sm;
     float2 *buf = sm + (n >> 1);
     for (int k = threadIdx.x; k < (n >> 1); k += blockDim.x) tw[k] = tw_g[k];
@@ -468,7 +469,12 @@ __device__ __forceinline__ void warp_inv_real(XFn x, bool sine, float2 *zb, cons
     }
 }
 
-// R1 (warp form): rows forward DCT-II, one warp per row.
+// R1 (warp form): rows forward DCT-II, one warp per row.  From the fixed-point
+// map, lane 0 of each warp first issues two bulk copies (the row's int64 sums
+// into the warp's work area, the row of the initial map into its stage area)
+// on the warp's mbarrier, so the whole row arrives at copy bandwidth while the
+// block loads the axis tables; the lanes then convert from shared memory and
+// zero the row with 16-byte stores.
 template <int E, int NW>
 __global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
     int m, const float2 *__restrict__ tw_n, const float2 *__restrict__ ek_n,
@@ -478,34 +484,62 @@ __global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
     DevState *__restrict__ st, double movable_area) {
     constexpr int H = 32 * E, N = 2 * H;
     if (st && st->done) return;
-    extern __shared__ float2 sm[];
-    const AxisTables tb = load_tables<NW, H>(sm, tw_n, ek_n);
+    extern __shared__ __align__(16) float2 sm[];
+    __shared__ __align__(8) uint64_t bar[NW];
+    __shared__ double shr[NW];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float2 *wbase = sm + tables_f2<H>() + warp * 2 * H;
+    const int row = blockIdx.x * NW + warp;
+    float2 *wbase = sm + tables_f2<H>() + warp * 3 * H;   // [2H float2 work | N float stage]
     float *xm = reinterpret_cast<float *>(wbase);
     float2 *zb = wbase + H;
-    __shared__ double shr[NW];
-    const int row = blockIdx.x * NW + warp;
-    double ovf = 0.0;
+    float *ini_s = reinterpret_cast<float *>(wbase + 2 * H);
     const bool from_map = rho_in == nullptr;
-#pragma unroll 8
-    for (int t = 0; t < 2 * E; ++t) {
-        const int i = lane + 32 * t;
-        const size_t idx = (size_t)row * N + i;
-        float v;
-        if (!from_map) {
-            v = rho_in[idx];
-        } else {
-            const unsigned long long q = dmap[idx];
-            if (zero_map) dmap[idx] = 0ull;
+    if (from_map && lane == 0) {
+        mbar_init(&bar[warp], 1);
+        mbar_expect_tx(&bar[warp], 12u * N);
+        bulk_load(wbase, dmap + (size_t)row * N, 8u * N, &bar[warp]);
+        bulk_load(ini_s, initial + (size_t)row * N, 4u * N, &bar[warp]);
+    }
+    __syncwarp();
+    const AxisTables tb = load_tables<NW, H>(sm, tw_n, ek_n);
+    double ovf = 0.0;
+    if (from_map) {
+        if (!mbar_wait(&bar[warp], 0)) {
+            if (lane == 0 && st) {
+                atomicOr(&st->status, kStatusWaitTimeout);
+                st->done = 1;
+            }
+            mbar_wait(&bar[warp], 0);   // the copy must land before the area is reused
+        }
+        const unsigned long long *q_s = reinterpret_cast<const unsigned long long *>(wbase);
+        float v[2 * E];
+#pragma unroll
+        for (int t = 0; t < 2 * E; ++t) {
+            const int i = lane + 32 * t;
             // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
-            const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q), fixed_inv), initial[idx]);
+            const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q_s[i]), fixed_inv), ini_s[i]);
             const float o = __fsub_rn(d, coef);
             ovf += (double)(o > 0.0f ? o : 0.0f);    // src/epotential.rs:274-276
-            v = __fmul_rn(d, inv_area);                // src/epotential.rs:284-285
-            if (rho_out) rho_out[idx] = v;
+            v[t] = __fmul_rn(d, inv_area);             // src/epotential.rs:284-285
         }
-        xm[makhoul_pos(i, N)] = v;
+        if (zero_map) {
+            ulonglong2 *zr = reinterpret_cast<ulonglong2 *>(dmap + (size_t)row * N);
+#pragma unroll
+            for (int k = 0; k < N / 64; ++k) zr[lane + 32 * k] = make_ulonglong2(0ull, 0ull);
+        }
+        if (rho_out) {
+#pragma unroll
+            for (int t = 0; t < 2 * E; ++t) rho_out[(size_t)row * N + lane + 32 * t] = v[t];
+        }
+        __syncwarp();   // every lane has read the staged row before xm overwrites it
+#pragma unroll
+        for (int t = 0; t < 2 * E; ++t) xm[makhoul_pos(lane + 32 * t, N)] = v[t];
+    } else {
+#pragma unroll 8
+        for (int t = 0; t < 2 * E; ++t) {
+            const int i = lane + 32 * t;
+            xm[makhoul_pos(i, N)] = rho_in[(size_t)row * N + i];
+        }
     }
     __syncthreads();   // twiddles + staged rows
     float *out = t1 + (size_t)row * N;
@@ -537,7 +571,7 @@ __global__ void __launch_bounds__(NW * 32) k_cols_w(
     constexpr int H = 32 * E, M = 2 * H;
     constexpr int S = NW + 1;   // tile row stride (odd: conflict-free row-wise access)
     if (st && st->done) return;
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     const AxisTables tb = load_tables<NW, H>(sm, tw_m, ek_m);
     const float2 *twh = tb.twh;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -621,7 +655,7 @@ __global__ void __launch_bounds__(NW * 32) k_rows_inv_w(
     const DevState *__restrict__ st) {
     constexpr int H = 32 * E, N = 2 * H;
     if (st && st->done) return;
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     const AxisTables tb = load_tables<NW, H>(sm, tw_n, ek_n);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float *xb = reinterpret_cast<float *>(sm + tables_f2<H>() + warp * 2 * H);
@@ -702,6 +736,8 @@ constexpr int kColWarps = 4;   // columns per block, warp kernels
 template <int E>
 static size_t rows_w_smem() { return sizeof(float2) * (size_t)(tables_f2<32 * E>() + kRowWarps * 64 * E); }
 template <int E>
+static size_t rows_dct_w_smem() { return sizeof(float2) * (size_t)(tables_f2<32 * E>() + kRowWarps * 96 * E); }
+template <int E>
 static size_t cols_w_smem() {
     return sizeof(float2) * (size_t)(tables_f2<32 * E>() + kColWarps * 96 * E) +
            sizeof(float) * (size_t)(64 * E) * (kColWarps + 2);
@@ -709,7 +745,7 @@ static size_t cols_w_smem() {
 
 template <int E>
 static cudaError_t prepare_w() {
-    cudaError_t e = cudaFuncSetAttribute(k_rows_dct_w<E, kRowWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_w_smem<E>());
+    cudaError_t e = cudaFuncSetAttribute(k_rows_dct_w<E, kRowWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_dct_w_smem<E>());
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_inv_w<E, kRowWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_w_smem<E>());
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cols_w<E, kColWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_w_smem<E>());
     return e;
@@ -739,7 +775,7 @@ static bool warp_side(int v) { return v >= 64 && v <= 2048; }
 
 template <int E>
 static void rows_dct_w(const SpectralPlan &p, const SpectralArgs &a, bool from_map) {
-    k_rows_dct_w<E, kRowWarps><<<p.m / kRowWarps, kRowWarps * 32, rows_w_smem<E>(), p.stream>>>(
+    k_rows_dct_w<E, kRowWarps><<<p.m / kRowWarps, kRowWarps * 32, rows_dct_w_smem<E>(), p.stream>>>(
         p.m, p.tw_n, p.ek_n, a.rho_in, a.dmap, a.initial, a.fixed_inv, a.coef, a.inv_bin_area,
         a.zero_map ? 1 : 0, a.rho_out, p.t1, from_map ? a.partials : nullptr, a.st, a.movable_area);
 }
