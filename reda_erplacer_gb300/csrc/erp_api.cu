@@ -291,7 +291,7 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
         cls_of[e] = k;
         counts[k]++;
     }
-    const int widths[kNumClasses] = {2, 4, 8, 16, 32, 32};
+    const int widths[kNumClasses] = {1, 1, 1, 2, 4, 32};   // lanes per net (k_wa's dispatch)
     int begin = 0;
     for (int k = 0; k < kNumClasses; ++k) {
         c.cls[k].begin = begin;
@@ -304,6 +304,11 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     for (int k = 0; k < kNumClasses; ++k) fill[k] = c.cls[k].begin;
     c.h_net_of_internal = new int32_t[E > 0 ? E : 1];
     for (int e = 0; e < E; ++e) c.h_net_of_internal[fill[cls_of[e]]++] = e;
+    for (int k = 0; k < kNumClasses; ++k)   // degree order within a class: warp-uniform pin loops
+        std::stable_sort(c.h_net_of_internal + c.cls[k].begin, c.h_net_of_internal + c.cls[k].begin + c.cls[k].count,
+                         [&](int32_t a, int32_t b) {
+                             return d->net_ptr[a + 1] - d->net_ptr[a] < d->net_ptr[b + 1] - d->net_ptr[b];
+                         });
     std::vector<int32_t> hnet_ptr(E + 1, 0), hslot_cell(P), hcell_ptr(NM + 1, 0);
     std::vector<float2> hslot_off(P);
     c.h_slot_of_pin = new int32_t[P > 0 ? P : 1];

@@ -15,12 +15,16 @@
 namespace erp {
 
 // ============================ wirelength ============================
-// One group of W lanes per net (nets sorted by degree class); lane l holds pins
-// l, l + W, ..., l + (P-1) W in registers, so positions are gathered and the
-// four max-shifted exponentials (src/hpwl.rs:285-299) evaluated once per pin
-// and reused for the gradient (the reference recomputes them,
-// src/hpwl.rs:314-333).  Nets with more than W*P pins fall back to a loop that
-// recomputes, like the reference.
+// One group of W lanes per net (nets sorted by degree class, and by degree
+// within a class); lane l holds pins l, l + W, ..., l + (P-1) W in registers, so
+// positions are gathered and the four max-shifted exponentials
+// (src/hpwl.rs:285-299) evaluated once per pin and reused for the gradient (the
+// reference recomputes them, src/hpwl.rs:314-333).  Nets of up to 8 pins take
+// one thread each (W = 1: no shuffles, the per-net coefficients computed once);
+// nets with more than W*P pins fall back to a loop that recomputes, like the
+// reference.  The weighted sums and the gradient use fused multiply-adds and
+// the four coefficient pairs one reciprocal each (src/hpwl.rs:304-312 divides
+// twice): ulp-level differences, inside the FP32 tolerance of the gradient.
 struct WaArgs {
     const int32_t *net_ptr;
     const int32_t *slot_cell;
@@ -92,8 +96,10 @@ __device__ __forceinline__ float wa_class(const WaArgs &a, int net_begin, int ne
                 enx[q] = expf((mnx - px[q]) * inv_gamma);
                 ey[q] = expf((py[q] - mxy) * inv_gamma);
                 eny[q] = expf((mny - py[q]) * inv_gamma);
-                s_xe += px[q] * ex[q]; s_xen += px[q] * enx[q]; s_e += ex[q]; s_en += enx[q];
-                s_ye += py[q] * ey[q]; s_yen += py[q] * eny[q]; s_f += ey[q]; s_fn += eny[q];
+                s_xe = __fmaf_rn(px[q], ex[q], s_xe); s_xen = __fmaf_rn(px[q], enx[q], s_xen);
+                s_e += ex[q]; s_en += enx[q];
+                s_ye = __fmaf_rn(py[q], ey[q], s_ye); s_yen = __fmaf_rn(py[q], eny[q], s_yen);
+                s_f += ey[q]; s_fn += eny[q];
             }
         }
         if (!in_regs) {
@@ -103,8 +109,8 @@ __device__ __forceinline__ float wa_class(const WaArgs &a, int net_begin, int ne
                 const float qx = a.x[c] + o.x, qy = a.y[c] + o.y;
                 const float e1 = expf((qx - mxx) * inv_gamma), e2 = expf((mnx - qx) * inv_gamma);
                 const float e3 = expf((qy - mxy) * inv_gamma), e4 = expf((mny - qy) * inv_gamma);
-                s_xe += qx * e1; s_xen += qx * e2; s_e += e1; s_en += e2;
-                s_ye += qy * e3; s_yen += qy * e4; s_f += e3; s_fn += e4;
+                s_xe = __fmaf_rn(qx, e1, s_xe); s_xen = __fmaf_rn(qx, e2, s_xen); s_e += e1; s_en += e2;
+                s_ye = __fmaf_rn(qy, e3, s_ye); s_yen = __fmaf_rn(qy, e4, s_yen); s_f += e3; s_fn += e4;
             }
         }
 #pragma unroll
@@ -118,18 +124,20 @@ __device__ __forceinline__ float wa_class(const WaArgs &a, int net_begin, int ne
             s_f += __shfl_xor_sync(0xffffffffu, s_f, o);
             s_fn += __shfl_xor_sync(0xffffffffu, s_fn, o);
         }
-        // src/hpwl.rs:304-312
-        const float one = 1.0f;
-        const float b_x = inv_gamma / s_e, a_x = (one - b_x * s_xe) / s_e;
-        const float b_nx = -inv_gamma / s_en, a_nx = (one - b_nx * s_xen) / s_en;
-        const float b_y = inv_gamma / s_f, a_y = (one - b_y * s_ye) / s_f;
-        const float b_ny = -inv_gamma / s_fn, a_ny = (one - b_ny * s_yen) / s_fn;
+        // src/hpwl.rs:304-312: b = +-1/(gamma s), a = (1 - b s_w) / s
+        const float r_e = __frcp_rn(s_e), r_en = __frcp_rn(s_en), r_f = __frcp_rn(s_f), r_fn = __frcp_rn(s_fn);
+        const float b_x = inv_gamma * r_e, a_x = __fmaf_rn(-b_x, s_xe, 1.0f) * r_e;
+        const float b_nx = -inv_gamma * r_en, a_nx = __fmaf_rn(-b_nx, s_xen, 1.0f) * r_en;
+        const float b_y = inv_gamma * r_f, a_y = __fmaf_rn(-b_y, s_ye, 1.0f) * r_f;
+        const float b_ny = -inv_gamma * r_fn, a_ny = __fmaf_rn(-b_ny, s_yen, 1.0f) * r_fn;
+        auto grad = [&](float qx, float qy, float e1, float e2, float e3, float e4) {
+            return make_float2(__fmaf_rn(__fmaf_rn(b_x, qx, a_x), e1, -(__fmaf_rn(b_nx, qx, a_nx) * e2)),
+                               __fmaf_rn(__fmaf_rn(b_y, qy, a_y), e3, -(__fmaf_rn(b_ny, qy, a_ny) * e4)));
+        };
 #pragma unroll
         for (int q = 0; q < P; ++q) {
             const int k = gl + q * W;
-            if (in_regs && k < deg)
-                a.slot_grad[s0 + k] = make_float2((a_x + b_x * px[q]) * ex[q] - (a_nx + b_nx * px[q]) * enx[q],
-                                                  (a_y + b_y * py[q]) * ey[q] - (a_ny + b_ny * py[q]) * eny[q]);
+            if (in_regs && k < deg) a.slot_grad[s0 + k] = grad(px[q], py[q], ex[q], enx[q], ey[q], eny[q]);
         }
         if (!in_regs) {
             for (int k = gl; k < deg; k += W) {
@@ -138,8 +146,7 @@ __device__ __forceinline__ float wa_class(const WaArgs &a, int net_begin, int ne
                 const float qx = a.x[c] + o.x, qy = a.y[c] + o.y;
                 const float e1 = expf((qx - mxx) * inv_gamma), e2 = expf((mnx - qx) * inv_gamma);
                 const float e3 = expf((qy - mxy) * inv_gamma), e4 = expf((mny - qy) * inv_gamma);
-                a.slot_grad[s0 + k] = make_float2((a_x + b_x * qx) * e1 - (a_nx + b_nx * qx) * e2,
-                                                  (a_y + b_y * qy) * e3 - (a_ny + b_ny * qy) * e4);
+                a.slot_grad[s0 + k] = grad(qx, qy, e1, e2, e3, e4);
             }
         }
         if (active && gl == 0) {
@@ -159,7 +166,7 @@ struct WaClasses {
     int block0[kNumClasses + 1];
 };
 
-__global__ void __launch_bounds__(kThreads) k_wa(WaArgs a, WaClasses cl, float gamma_arg,
+__global__ void __launch_bounds__(kThreads, 3) k_wa(WaArgs a, WaClasses cl, float gamma_arg,
                                                  double *__restrict__ partials, DevState *st) {
     __shared__ double shr[kThreads / 32];
     if (st->done) return;
@@ -170,11 +177,11 @@ __global__ void __launch_bounds__(kThreads) k_wa(WaArgs a, WaClasses cl, float g
     const int cb = blockIdx.x - cl.block0[k], cg = cl.block0[k + 1] - cl.block0[k];
     float hp;
     switch (k) {
-    case 0: hp = wa_class<2, 1>(a, cl.begin[0], cl.count[0], cl.general[0], cb, cg); break;
-    case 1: hp = wa_class<4, 1>(a, cl.begin[1], cl.count[1], cl.general[1], cb, cg); break;
-    case 2: hp = wa_class<8, 1>(a, cl.begin[2], cl.count[2], cl.general[2], cb, cg); break;
-    case 3: hp = wa_class<16, 1>(a, cl.begin[3], cl.count[3], cl.general[3], cb, cg); break;
-    case 4: hp = wa_class<32, 1>(a, cl.begin[4], cl.count[4], cl.general[4], cb, cg); break;
+    case 0: hp = wa_class<1, 2>(a, cl.begin[0], cl.count[0], cl.general[0], cb, cg); break;
+    case 1: hp = wa_class<1, 4>(a, cl.begin[1], cl.count[1], cl.general[1], cb, cg); break;
+    case 2: hp = wa_class<1, 8>(a, cl.begin[2], cl.count[2], cl.general[2], cb, cg); break;
+    case 3: hp = wa_class<2, 8>(a, cl.begin[3], cl.count[3], cl.general[3], cb, cg); break;
+    case 4: hp = wa_class<4, 8>(a, cl.begin[4], cl.count[4], cl.general[4], cb, cg); break;
     default: hp = wa_class<32, 4>(a, cl.begin[5], cl.count[5], cl.general[5], cb, cg); break;
     }
     const double b = block_sum((double)hp, shr);

@@ -9,7 +9,8 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "liberplacer_gb300.so")
+# ERP_LIBRARY names another build of the same ABI (e.g. one compiled elsewhere).
+LIB_PATH = os.environ.get("ERP_LIBRARY") or os.path.join(HERE, "liberplacer_gb300.so")
 
 f32p = C.POINTER(C.c_float)
 i32p = C.POINTER(C.c_int32)
