@@ -154,6 +154,7 @@ struct SpectralArgs {
 };
 void launch_spectral_plan(const SpectralPlan &p, const SpectralArgs &a);
 cudaError_t spectral_prepare();
+cudaError_t place_prepare();   // opt the density scatter into its dynamic shared memory
 size_t spectral_smem_bytes(int m, int n);
 
 int ilog2(int v);

@@ -9,6 +9,8 @@
 // CPU replay of the same rule.
 #include <math.h>
 
+#include <algorithm>
+
 #include "erp_internal.cuh"
 #include "reduce.cuh"
 
@@ -244,33 +246,49 @@ __device__ __forceinline__ float tri_clamped(float x, float s, int k, float bs) 
 // changes no bit of the result:
 //  * each block owns a kWin x kWin bin window in shared memory anchored at its
 //    first cell; contributions inside it are accumulated there and flushed with
-//    one global atomic per touched bin, the rest go to global memory directly.
+//    one global atomic per touched bin, the rest go to global memory directly;
+//  * a contribution c in [0, 2^63) is kept in the window as three 21-bit pieces
+//    in three 32-bit planes (32-bit shared atomics are native; 64-bit ones are
+//    several times slower and degrade under contention).  A bin receives at
+//    most one contribution per cell and a block owns at most kMaxCellsPerBlock
+//    = 2^11 cells, so each plane's sum stays below 2^32 and the flush
+//    recombines the exact 64-bit total;
+//  * contributions outside the window go to a per-block table of kTable bins
+//    (the slot a bin hashes to, claimed by the first bin that reaches it; a
+//    bin whose slot is taken goes to global memory), so bins that many of the
+//    block's cells share -- late in a diverging run cells pile up along the die
+//    edge -- cost one global atomic per block.
 // Early on all cells sit within a few bins of the die centre, where this turns
 // millions of contended global atomics into a few per block.
 constexpr int kWin = 64;
+constexpr int kTableLog = 9, kTable = 1 << kTableLog;   // out-of-window bin table (open, no probing)
+constexpr unsigned kEmpty = 0xffffffffu;                 // bin indices are < 4096 * 4096
+constexpr int kMaxCellsPerBlock = 2048;
+constexpr unsigned long long kPiece = (1ull << 21) - 1;
 __global__ void __launch_bounds__(kThreads) k_density_scatter(
     int NM, const float *__restrict__ x, const float *__restrict__ y,
     const float *__restrict__ offx, const float *__restrict__ offy, const float *__restrict__ cw,
     const float *__restrict__ ch, const float *__restrict__ ratio, int m, int n, float bw,
     float bh, float inv_bw, float inv_bh, float scale, unsigned long long *__restrict__ map,
     const DevState *__restrict__ st) {
-    __shared__ unsigned long long win[kWin * kWin];
-    __shared__ int s_org[2];
+    extern __shared__ unsigned dsm[];
+    unsigned *win = dsm;                            // window planes: bits 0-20, 21-41, 42-62
+    unsigned *tkey = dsm + 3 * kWin * kWin;          // bin table: keys (bin index or kEmpty)
+    unsigned *tplane = tkey + kTable;                // bin table: planes
     if (st->done) return;
-    const int per = ((NM + gridDim.x - 1) / gridDim.x + 31) & ~31;
+    const int per = ((NM + gridDim.x - 1) / gridDim.x + 31) & ~31;   // <= kMaxCellsPerBlock (launcher)
     const int c0 = blockIdx.x * per, c1 = min(c0 + per, NM);
-    if (threadIdx.x == 0) {
-        int ox = 0, oy = 0;
-        if (c0 < NM) {
-            ox = (int)floorf(clamp_bin((x[c0] + offx[c0]) * inv_bw, m)) - kWin / 2;
-            oy = (int)floorf(clamp_bin((y[c0] + offy[c0]) * inv_bh, n)) - kWin / 2;
-        }
-        s_org[0] = max(0, min(ox, m - kWin));
-        s_org[1] = max(0, min(oy, n - kWin));
+    int wox = 0, woy = 0;   // window origin: every thread derives it from the block's first cell
+    if (c0 < NM) {
+        wox = (int)floorf(clamp_bin((x[c0] + offx[c0]) * inv_bw, m)) - kWin / 2;
+        woy = (int)floorf(clamp_bin((y[c0] + offy[c0]) * inv_bh, n)) - kWin / 2;
     }
-    for (int k = threadIdx.x; k < kWin * kWin; k += blockDim.x) win[k] = 0ull;
+    wox = max(0, min(wox, m - kWin));
+    woy = max(0, min(woy, n - kWin));
+    for (int k = threadIdx.x; k < 3 * kWin * kWin; k += blockDim.x) win[k] = 0u;
+    for (int k = threadIdx.x; k < kTable; k += blockDim.x) tkey[k] = kEmpty;
+    for (int k = threadIdx.x; k < 3 * kTable; k += blockDim.x) tplane[k] = 0u;
     __syncthreads();
-    const int wox = s_org[0], woy = s_org[1];
     for (int base = c0; base < c1; base += blockDim.x) {
         const int i = base + threadIdx.x;
         int bxl = 0, byl = 0, nx = 0, ny = 0;
@@ -291,27 +309,68 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
             nx = max(xh - xl, 0);
             ny = max(yh - yl, 0);
         }
-        const int cnt = nx * ny;
-        for (int k = 0; k < cnt; ++k) {
-            const int dx = k / ny, dy = k - dx * ny;
-            const int bx = bxl + dx, by = byl + dy;
-            const float px = r * tri_clamped(xi, sxi, bx, bw);
-            const float py = tri_clamped(yi, syi, by, bh);
-            const long long c = __float2ll_rn((px * py) * scale);
-            if (!c) continue;
+        auto add = [&](int bx, int by, unsigned long long c) {
             const int wx = bx - wox, wy = by - woy;
-            if (wx >= 0 && wx < kWin && wy >= 0 && wy < kWin)
-                atomicAdd(win + wx * kWin + wy, (unsigned long long)c);
-            else
-                atomicAdd(map + (size_t)bx * n + by, (unsigned long long)c);
+            if (wx >= 0 && wx < kWin && wy >= 0 && wy < kWin) {
+                unsigned *w = win + wx * kWin + wy;
+                atomicAdd(w, (unsigned)(c & kPiece));
+                if (c >> 21) {
+                    atomicAdd(w + kWin * kWin, (unsigned)((c >> 21) & kPiece));
+                    if (c >> 42) atomicAdd(w + 2 * kWin * kWin, (unsigned)(c >> 42));
+                }
+            } else {   // outside the window: the block's bin table, else global memory
+                const unsigned bin = (unsigned)bx * (unsigned)n + (unsigned)by;
+                const unsigned slot = (bin * 2654435761u) >> (32 - kTableLog);
+                unsigned k = tkey[slot];
+                if (k == kEmpty) {
+                    k = atomicCAS(tkey + slot, kEmpty, bin);
+                    if (k == kEmpty) k = bin;
+                }
+                if (k == bin) {
+                    unsigned *t = tplane + slot;
+                    atomicAdd(t, (unsigned)(c & kPiece));
+                    if (c >> 21) {
+                        atomicAdd(t + kTable, (unsigned)((c >> 21) & kPiece));
+                        if (c >> 42) atomicAdd(t + 2 * kTable, (unsigned)(c >> 42));
+                    }
+                } else {
+                    atomicAdd(map + bin, c);
+                }
+            }
+        };
+        for (int dx = 0; dx < nx; ++dx) {
+            const int bx = bxl + dx;
+            const float px = r * tri_clamped(xi, sxi, bx, bw);
+            if (px == 0.0f) continue;   // every contribution of this bin column is 0
+            for (int dy = 0; dy < ny; ++dy) {
+                const int by = byl + dy;
+                const float py = tri_clamped(yi, syi, by, bh);
+                const unsigned long long c = (unsigned long long)__float2ll_rn((px * py) * scale);
+                if (c) add(bx, by, c);
+            }
         }
     }
     __syncthreads();
     for (int k = threadIdx.x; k < kWin * kWin; k += blockDim.x) {
-        const unsigned long long v = win[k];
+        const unsigned long long v = (unsigned long long)win[k] + ((unsigned long long)win[k + kWin * kWin] << 21) +
+                                     ((unsigned long long)win[k + 2 * kWin * kWin] << 42);
         const int bx = wox + k / kWin, by = woy + k % kWin;
         if (v && bx < m && by < n) atomicAdd(map + (size_t)bx * n + by, v);
     }
+    for (int k = threadIdx.x; k < kTable; k += blockDim.x) {
+        const unsigned bin = tkey[k];
+        if (bin == kEmpty) continue;
+        const unsigned long long v = (unsigned long long)tplane[k] + ((unsigned long long)tplane[k + kTable] << 21) +
+                                     ((unsigned long long)tplane[k + 2 * kTable] << 42);
+        if (v) atomicAdd(map + bin, v);
+    }
+}
+
+size_t density_scatter_smem() { return sizeof(unsigned) * (3 * kWin * kWin + 4 * kTable); }
+
+cudaError_t place_prepare() {
+    return cudaFuncSetAttribute(k_density_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)density_scatter_smem());
 }
 
 // compute_density_overflow (src/density.rs:16-23): overlap through bin centres
@@ -704,7 +763,8 @@ void launch_wl_gather(Ctx &c) {
 }
 
 void launch_density_scatter(Ctx &c) {
-    k_density_scatter<<<grid_for(c.NM, 152 * 4), kThreads, 0, c.stream>>>(
+    const int g = std::max(grid_for(c.NM, 152 * 4), (c.NM + kMaxCellsPerBlock - 1) / kMaxCellsPerBlock);
+    k_density_scatter<<<g, kThreads, density_scatter_smem(), c.stream>>>(
         c.NM, c.x, c.y, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw,
         c.inv_bh, c.fixed_scale, c.dmap, c.st);
 }
