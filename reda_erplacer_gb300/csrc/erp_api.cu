@@ -146,7 +146,7 @@ erp_status validate(const erp_design *d, std::string &err) {
 }
 
 void free_ctx(Ctx &c) {
-    void *ptrs[] = {c.x, c.y, c.w, c.h, c.npins, c.cw, c.ch, c.offx, c.offy, c.ratio, c.wlgx, c.wlgy,
+    void *ptrs[] = {c.x, c.y, c.xy, c.w, c.h, c.npins, c.cw, c.ch, c.offx, c.offy, c.ratio, c.wlgx, c.wlgy,
                     c.dgx, c.dgy, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.slot_cell, c.slot_off,
                     c.slot_grad, c.net_ptr, c.net_hpwl, c.cell_slot_ptr, c.cell_slots, c.dmap,
                     c.initial, c.rho, c.t1, c.tx, c.ty, c.tp, c.fx, c.fy, c.psi, c.tw_m, c.tw_n,
@@ -283,22 +283,22 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     for (int e = 0; e < E; ++e) {
         const int deg = d->net_ptr[e + 1] - d->net_ptr[e];
         int k;
-        if (e < d->n_2nets) k = 0;
-        else if (deg <= 4) k = 1;
-        else if (deg <= 8) k = 2;
-        else if (deg <= 16) k = 3;
-        else if (deg <= 32) k = 4;
-        else k = 5;
+        if (e < d->n_2nets) k = 0;                       // validated: exactly 2 pins
+        else if (deg >= 2 && deg <= kNumExact) k = deg - 1;
+        else if (deg <= 16) k = kNumExact;
+        else if (deg <= 32) k = kNumExact + 1;
+        else k = kNumExact + 2;
         cls_of[e] = k;
         counts[k]++;
     }
-    const int widths[kNumClasses] = {1, 1, 1, 2, 4, 32};   // lanes per net (k_wa's dispatch)
+    const int widths[kNumClasses] = {1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 32};   // lanes per net (k_wa's dispatch)
     int begin = 0;
     for (int k = 0; k < kNumClasses; ++k) {
         c.cls[k].begin = begin;
         c.cls[k].count = counts[k];
         c.cls[k].width = widths[k];
         c.cls[k].general = k == 0 ? 0 : 1;
+        c.cls[k].degree = k == 0 ? 2 : (k < kNumExact ? k + 1 : 0);
         begin += counts[k];
     }
     std::vector<int> fill(kNumClasses);
@@ -315,10 +315,21 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     c.h_slot_of_pin = new int32_t[P > 0 ? P : 1];
     for (int p = 0; p < P; ++p) c.h_slot_of_pin[p] = -1;
     int slot = 0;
-    for (int ie = 0; ie < E; ++ie) {
-        const int e = c.h_net_of_internal[ie];
-        hnet_ptr[ie] = slot;
-        for (int k = d->net_ptr[e]; k < d->net_ptr[e + 1]; ++k) c.h_slot_of_pin[d->net_pins[k]] = slot++;
+    for (int k = 0; k < kNumClasses; ++k) {
+        NetClass &nc = c.cls[k];
+        nc.slot0 = slot;
+        for (int g = 0; g < nc.count; ++g) {
+            const int ie = nc.begin + g, e = c.h_net_of_internal[ie];
+            if (nc.degree) {   // pin-major: pin q of net g at slot0 + q * count + g
+                hnet_ptr[ie] = nc.slot0 + g;
+                for (int q = 0; q < nc.degree; ++q)
+                    c.h_slot_of_pin[d->net_pins[d->net_ptr[e] + q]] = nc.slot0 + q * nc.count + g;
+            } else {
+                hnet_ptr[ie] = slot;
+                for (int p = d->net_ptr[e]; p < d->net_ptr[e + 1]; ++p) c.h_slot_of_pin[d->net_pins[p]] = slot++;
+            }
+        }
+        if (nc.degree) slot += nc.degree * nc.count;
     }
     hnet_ptr[E] = slot;
     for (int p = 0; p < P; ++p)
@@ -339,6 +350,7 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
                          &c.wlgx, &c.wlgy, &c.dgx, &c.dgy, &c.prev_x, &c.prev_y, &c.prev_gx, &c.prev_gy};
     cudaStream_t s0 = c.stream;
     for (float **a : cellarr) CK(dalloc(a, (size_t)N + 4, s0));
+    CK(dalloc(&c.xy, (size_t)N + 4, s0));
     CK(dalloc(&c.slot_cell, P, s0));
     CK(dalloc(&c.slot_off, P, s0));
     CK(dalloc(&c.slot_grad, P, s0));
@@ -389,6 +401,7 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     h.beta = 0.0f;
     *c.h_st = h;
     CK(cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream));
+    launch_pack_xy(c);
     // fixed-cell initial density (src/epotential.rs:127-140)
     launch_initial_density(c, nullptr, nullptr, nullptr, nullptr);
     CK(cudaGetLastError());
@@ -586,6 +599,7 @@ extern "C" erp_status erp_step_host(erp_ctx *ctx, float *x, float *y, erp_step_s
     if (!x || !y) return ERP_EINVAL;
     CK(cudaMemcpyAsync(c.x, x, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
     CK(cudaMemcpyAsync(c.y, y, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+    launch_pack_xy(c);
     erp_status s = enqueue_step(c);
     if (s != ERP_OK) return s;
     CK(cudaMemcpyAsync(x, c.x, sizeof(float) * c.N, cudaMemcpyDeviceToHost, c.stream));
@@ -691,6 +705,8 @@ extern "C" erp_status erp_set_positions(erp_ctx *ctx, const float *x, const floa
     if (!x || !y) return ERP_EINVAL;
     CK(cudaMemcpyAsync(c.x, x, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
     CK(cudaMemcpyAsync(c.y, y, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+    launch_pack_xy(c);
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c.stream));
     return ERP_OK;
 }

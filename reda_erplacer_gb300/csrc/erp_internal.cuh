@@ -52,11 +52,20 @@ constexpr int32_t kStatusWaitTimeout = 2;   // DevState::status bit 1
 enum Counter { CTR_HPWL = 0, CTR_OVF = 1, CTR_ABS = 2, CTR_LIP = 3, CTR_ENERGY = 4 };
 
 // Net degree classes processed by one thread group of width W each.
-constexpr int kNumClasses = 6;  // fast 2-pin, <=4, <=8, <=16, <=32, >32
+// Classes 0..7 hold nets of one exact degree -- class 0 the leading 2-pin nets
+// (the reference's fast path), classes 1..7 the other nets of degree 2..8 --
+// whose pin slots are stored pin-major: pin q of the class's net g sits at slot
+// slot0 + q * count + g, so one thread per net reads and writes coalesced.
+// Classes 8..10 hold the remaining nets (degree <= 16, <= 32, > 32) with each
+// net's slots contiguous (net_ptr), served by lane groups.
+constexpr int kNumExact = 8;
+constexpr int kNumClasses = 11;
 struct NetClass {
     int32_t begin, count;  // range in the internal net order
     int32_t width;         // lanes per net
     int32_t general;       // 1: general path (min/max initialised to die+1 / 0)
+    int32_t degree;        // exact degree (classes 0..7), else 0
+    int32_t slot0;         // first pin slot of the class
 };
 
 struct Ctx {
@@ -73,6 +82,7 @@ struct Ctx {
     std::string err;
     // --- cells [N] ---
     float *x, *y, *w, *h, *npins, *cw, *ch, *offx, *offy, *ratio;
+    float2 *xy;                // (x, y) interleaved: one 8-byte gather per pin in the wirelength pass
     float *wlgx, *wlgy, *dgx, *dgy;
     float *prev_x, *prev_y, *prev_gx, *prev_gy;
     // --- pins in internal slot order [NS] ---
@@ -111,6 +121,7 @@ constexpr int kMaxPartials = 8192;
 // ---------------- launchers (stream = ctx.stream) ----------------
 // wirelength (src/hpwl.rs)
 void launch_wirelength(Ctx &c, float gamma_arg);          // gamma_arg < 0: read DevState.gamma
+void launch_pack_xy(Ctx &c);                               // xy from x, y after a host write
 void launch_wl_gather(Ctx &c);
 // density + spectral + force (src/density.rs, src/epotential.rs, src/eforce.rs)
 void launch_initial_density(Ctx &c, const float *hx, const float *hy, const float *hw,

@@ -31,7 +31,7 @@ struct WaArgs {
     const int32_t *net_ptr;
     const int32_t *slot_cell;
     const float2 *slot_off;
-    const float *x, *y;
+    const float2 *xy;
     float2 *slot_grad;
     float *net_hpwl;
     float inv_gamma, def_min_x, def_min_y;
@@ -61,8 +61,9 @@ __device__ __forceinline__ float wa_class(const WaArgs &a, int net_begin, int ne
             if (in_regs && k < deg) {
                 const int c = a.slot_cell[s0 + k];
                 const float2 o = a.slot_off[s0 + k];
-                px[q] = a.x[c] + o.x;                       // src/hpwl.rs:107
-                py[q] = a.y[c] + o.y;
+                const float2 p = a.xy[c];
+                px[q] = p.x + o.x;                          // src/hpwl.rs:107
+                py[q] = p.y + o.y;
                 mnx = fminf(mnx, px[q]); mxx = fmaxf(mxx, px[q]);
                 mny = fminf(mny, py[q]); mxy = fmaxf(mxy, py[q]);
             }
@@ -71,7 +72,8 @@ __device__ __forceinline__ float wa_class(const WaArgs &a, int net_begin, int ne
             for (int k = gl; k < deg; k += W) {
                 const int c = a.slot_cell[s0 + k];
                 const float2 o = a.slot_off[s0 + k];
-                const float qx = a.x[c] + o.x, qy = a.y[c] + o.y;
+                const float2 p = a.xy[c];
+                const float qx = p.x + o.x, qy = p.y + o.y;
                 mnx = fminf(mnx, qx); mxx = fmaxf(mxx, qx);
                 mny = fminf(mny, qy); mxy = fmaxf(mxy, qy);
             }
@@ -108,7 +110,8 @@ __device__ __forceinline__ float wa_class(const WaArgs &a, int net_begin, int ne
             for (int k = gl; k < deg; k += W) {
                 const int c = a.slot_cell[s0 + k];
                 const float2 o = a.slot_off[s0 + k];
-                const float qx = a.x[c] + o.x, qy = a.y[c] + o.y;
+                const float2 p = a.xy[c];
+                const float qx = p.x + o.x, qy = p.y + o.y;
                 const float e1 = expf((qx - mxx) * inv_gamma), e2 = expf((mnx - qx) * inv_gamma);
                 const float e3 = expf((qy - mxy) * inv_gamma), e4 = expf((mny - qy) * inv_gamma);
                 s_xe = __fmaf_rn(qx, e1, s_xe); s_xen = __fmaf_rn(qx, e2, s_xen); s_e += e1; s_en += e2;
@@ -145,7 +148,8 @@ __device__ __forceinline__ float wa_class(const WaArgs &a, int net_begin, int ne
             for (int k = gl; k < deg; k += W) {
                 const int c = a.slot_cell[s0 + k];
                 const float2 o = a.slot_off[s0 + k];
-                const float qx = a.x[c] + o.x, qy = a.y[c] + o.y;
+                const float2 p = a.xy[c];
+                const float qx = p.x + o.x, qy = p.y + o.y;
                 const float e1 = expf((qx - mxx) * inv_gamma), e2 = expf((mnx - qx) * inv_gamma);
                 const float e3 = expf((qy - mxy) * inv_gamma), e4 = expf((mny - qy) * inv_gamma);
                 a.slot_grad[s0 + k] = grad(qx, qy, e1, e2, e3, e4);
@@ -160,11 +164,69 @@ __device__ __forceinline__ float wa_class(const WaArgs &a, int net_begin, int ne
     return hp_acc;
 }
 
+// One thread per net of exact degree D, pins stored pin-major (pin q of the
+// class's net g at slot0 + q * count + g): the slot reads and gradient writes of
+// a warp are coalesced and no net_ptr is read.  Same arithmetic as wa_class.
+template <int D>
+__device__ __forceinline__ float wa_exact(const WaArgs &a, int net_begin, int net_count, int slot0,
+                                          int general, int cblock, int cgrid) {
+    const float inv_gamma = a.inv_gamma;
+    float hp_acc = 0.0f;
+    for (int g = cblock * kThreads + (int)threadIdx.x; g < net_count; g += cgrid * kThreads) {
+        float px[D], py[D];
+        float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
+#pragma unroll
+        for (int q = 0; q < D; ++q) {
+            const int sl = slot0 + q * net_count + g;
+            const int c = a.slot_cell[sl];
+            const float2 o = a.slot_off[sl];
+            const float2 p = a.xy[c];
+            px[q] = p.x + o.x;                              // src/hpwl.rs:107
+            py[q] = p.y + o.y;
+            mnx = fminf(mnx, px[q]); mxx = fmaxf(mxx, px[q]);
+            mny = fminf(mny, py[q]); mxy = fmaxf(mxy, py[q]);
+        }
+        if (general) {  // src/hpwl.rs:255-258 initial values
+            mnx = fminf(a.def_min_x, mnx); mxx = fmaxf(0.0f, mxx);
+            mny = fminf(a.def_min_y, mny); mxy = fmaxf(0.0f, mxy);
+        }
+        float ex[D], enx[D], ey[D], eny[D];
+        float s_xe = 0.f, s_xen = 0.f, s_e = 0.f, s_en = 0.f;
+        float s_ye = 0.f, s_yen = 0.f, s_f = 0.f, s_fn = 0.f;
+#pragma unroll
+        for (int q = 0; q < D; ++q) {
+            ex[q] = expf((px[q] - mxx) * inv_gamma);
+            enx[q] = expf((mnx - px[q]) * inv_gamma);
+            ey[q] = expf((py[q] - mxy) * inv_gamma);
+            eny[q] = expf((mny - py[q]) * inv_gamma);
+            s_xe = __fmaf_rn(px[q], ex[q], s_xe); s_xen = __fmaf_rn(px[q], enx[q], s_xen);
+            s_e += ex[q]; s_en += enx[q];
+            s_ye = __fmaf_rn(py[q], ey[q], s_ye); s_yen = __fmaf_rn(py[q], eny[q], s_yen);
+            s_f += ey[q]; s_fn += eny[q];
+        }
+        // src/hpwl.rs:304-312: b = +-1/(gamma s), a = (1 - b s_w) / s
+        const float r_e = __frcp_rn(s_e), r_en = __frcp_rn(s_en), r_f = __frcp_rn(s_f), r_fn = __frcp_rn(s_fn);
+        const float b_x = inv_gamma * r_e, a_x = __fmaf_rn(-b_x, s_xe, 1.0f) * r_e;
+        const float b_nx = -inv_gamma * r_en, a_nx = __fmaf_rn(-b_nx, s_xen, 1.0f) * r_en;
+        const float b_y = inv_gamma * r_f, a_y = __fmaf_rn(-b_y, s_ye, 1.0f) * r_f;
+        const float b_ny = -inv_gamma * r_fn, a_ny = __fmaf_rn(-b_ny, s_yen, 1.0f) * r_fn;
+#pragma unroll
+        for (int q = 0; q < D; ++q)
+            a.slot_grad[slot0 + q * net_count + g] =
+                make_float2(__fmaf_rn(__fmaf_rn(b_x, px[q], a_x), ex[q], -(__fmaf_rn(b_nx, px[q], a_nx) * enx[q])),
+                            __fmaf_rn(__fmaf_rn(b_y, py[q], a_y), ey[q], -(__fmaf_rn(b_ny, py[q], a_ny) * eny[q])));
+        const float hp = (mxx - mnx) + (mxy - mny);   // src/hpwl.rs:302
+        a.net_hpwl[net_begin + g] = hp;
+        hp_acc += hp;
+    }
+    return hp_acc;
+}
+
 // All degree classes in one launch: blocks [cls_block[k], cls_block[k+1]) serve
 // class k.  The block partials of the HPWL total are summed in FP64 by the last
 // block to finish (fixed order, src/hpwl.rs:341-342).
 struct WaClasses {
-    int begin[kNumClasses], count[kNumClasses], general[kNumClasses];
+    int begin[kNumClasses], count[kNumClasses], general[kNumClasses], slot0[kNumClasses];
     int block0[kNumClasses + 1];
 };
 
@@ -178,14 +240,22 @@ __global__ void __launch_bounds__(kThreads, 3) k_wa(WaArgs a, WaClasses cl, floa
     while (k + 1 < kNumClasses && (int)blockIdx.x >= cl.block0[k + 1]) ++k;
     const int cb = blockIdx.x - cl.block0[k], cg = cl.block0[k + 1] - cl.block0[k];
     float hp;
+#define ERP_WA_EXACT(K, D) \
+    case K: hp = wa_exact<D>(a, cl.begin[K], cl.count[K], cl.slot0[K], cl.general[K], cb, cg); break;
     switch (k) {
-    case 0: hp = wa_class<1, 2>(a, cl.begin[0], cl.count[0], cl.general[0], cb, cg); break;
-    case 1: hp = wa_class<1, 4>(a, cl.begin[1], cl.count[1], cl.general[1], cb, cg); break;
-    case 2: hp = wa_class<1, 8>(a, cl.begin[2], cl.count[2], cl.general[2], cb, cg); break;
-    case 3: hp = wa_class<2, 8>(a, cl.begin[3], cl.count[3], cl.general[3], cb, cg); break;
-    case 4: hp = wa_class<4, 8>(a, cl.begin[4], cl.count[4], cl.general[4], cb, cg); break;
-    default: hp = wa_class<32, 4>(a, cl.begin[5], cl.count[5], cl.general[5], cb, cg); break;
+    ERP_WA_EXACT(0, 2)
+    ERP_WA_EXACT(1, 2)
+    ERP_WA_EXACT(2, 3)
+    ERP_WA_EXACT(3, 4)
+    ERP_WA_EXACT(4, 5)
+    ERP_WA_EXACT(5, 6)
+    ERP_WA_EXACT(6, 7)
+    ERP_WA_EXACT(7, 8)
+    case 8: hp = wa_class<2, 8>(a, cl.begin[8], cl.count[8], cl.general[8], cb, cg); break;
+    case 9: hp = wa_class<4, 8>(a, cl.begin[9], cl.count[9], cl.general[9], cb, cg); break;
+    default: hp = wa_class<32, 4>(a, cl.begin[10], cl.count[10], cl.general[10], cb, cg); break;
     }
+#undef ERP_WA_EXACT
     const double b = block_sum((double)hp, shr);
     double vals[1] = {b};
     if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_HPWL], gridDim.x)) {
@@ -633,7 +703,8 @@ __device__ __forceinline__ void nesterov_update_cell(float &x, float &y, float &
 __global__ void __launch_bounds__(kThreads) k_nesterov_update(
     int NM, const float *__restrict__ w, const float *__restrict__ h, float die_w, float die_h,
     float *__restrict__ x, float *__restrict__ y, float *__restrict__ px, float *__restrict__ py,
-    const float *__restrict__ gx, const float *__restrict__ gy, const DevState *__restrict__ st) {
+    const float *__restrict__ gx, const float *__restrict__ gy, float2 *__restrict__ xy,
+    const DevState *__restrict__ st) {
     if (st->done) return;
     const float alpha = st->alpha, beta = st->beta;
     const int n4 = NM >> 2;
@@ -648,6 +719,9 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_update(
         st4(y, i4, yy);
         st4(px, i4, qx);
         st4(py, i4, qy);
+        float4 *xy4 = reinterpret_cast<float4 *>(xy) + 2 * i4;
+        xy4[0] = make_float4(xx.v[0], yy.v[0], xx.v[1], yy.v[1]);
+        xy4[1] = make_float4(xx.v[2], yy.v[2], xx.v[3], yy.v[3]);
     }
     if (blockIdx.x == 0 && threadIdx.x < (NM & 3)) {
         const int i = (n4 << 2) + threadIdx.x;
@@ -657,7 +731,15 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_update(
         y[i] = yi;
         px[i] = pxi;
         py[i] = pyi;
+        xy[i] = make_float2(xi, yi);
     }
+}
+
+// xy = (x, y) for every instance, after positions were written from the host.
+__global__ void k_pack_xy(int N, const float *__restrict__ x, const float *__restrict__ y,
+                          float2 *__restrict__ xy) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+        xy[i] = make_float2(x[i], y[i]);
 }
 
 // ============================ scheduler ============================
@@ -729,8 +811,7 @@ void launch_wirelength(Ctx &c, float gamma_arg) {
     a.net_ptr = c.net_ptr;
     a.slot_cell = c.slot_cell;
     a.slot_off = c.slot_off;
-    a.x = c.x;
-    a.y = c.y;
+    a.xy = c.xy;
     a.slot_grad = c.slot_grad;
     a.net_hpwl = c.net_hpwl;
     a.inv_gamma = 0.f;
@@ -743,6 +824,7 @@ void launch_wirelength(Ctx &c, float gamma_arg) {
         cl.begin[k] = nc.begin;
         cl.count[k] = nc.count;
         cl.general[k] = nc.general;
+        cl.slot0[k] = nc.slot0;
         cl.block0[k] = blocks;
         const int gpb = kThreads / nc.width;
         int g = (nc.count + gpb - 1) / gpb;
@@ -822,7 +904,11 @@ void launch_nesterov(Ctx &c, int iter_arg) {
                                                   c.h, c.npins, c.x, c.y, c.prev_x, c.prev_y,
                                                   c.prev_gx, c.prev_gy, c.partials, c.st);
     k_nesterov_update<<<g4, kThreads, 0, c.stream>>>(c.NM, c.w, c.h, c.die_w, c.die_h, c.x, c.y,
-                                                    c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.st);
+                                                    c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.xy, c.st);
+}
+
+void launch_pack_xy(Ctx &c) {
+    if (c.N > 0) k_pack_xy<<<grid_for(c.N), kThreads, 0, c.stream>>>(c.N, c.x, c.y, c.xy);
 }
 
 void launch_scheduler(Ctx &c, int use_args, float hpwl, float overflow) {
