@@ -321,7 +321,8 @@ __host__ __device__ constexpr int brev_c(int v) {
     return r;
 }
 
-template <int E, bool INV>
+// tw holds W_{S N}^k (k < S N / 2); the N-point transform uses W_N^i = tw[S i].
+template <int E, bool INV, int S = 1>
 __device__ __forceinline__ void warp_fft(float2 (&r)[E], const float2 *__restrict__ tw, int lane) {
     constexpr int N = 32 * E;
     // 1. registers
@@ -331,7 +332,7 @@ __device__ __forceinline__ void warp_fft(float2 (&r)[E], const float2 *__restric
         for (int i0 = 0; i0 < E; ++i0) {
             if (i0 & h) continue;
             const int i1 = i0 + h, j = i0 & (h - 1);
-            float2 w = tw[32 * j * (E / (2 * h))];
+            float2 w = tw[S * 32 * j * (E / (2 * h))];
             if (INV) w.y = -w.y;
             const float2 u = r[i0], v = r[i1];
             r[i0] = make_float2(u.x + v.x, u.y + v.y);
@@ -344,7 +345,7 @@ __device__ __forceinline__ void warp_fft(float2 (&r)[E], const float2 *__restric
         const int q = brev_c<E>(j);
         if (q == 0) continue;
         const int idx = lane * q;
-        float2 w = idx < N / 2 ? tw[idx] : tw[idx - N / 2];
+        float2 w = idx < N / 2 ? tw[S * idx] : tw[S * (idx - N / 2)];
         if (idx >= N / 2) { w.x = -w.x; w.y = -w.y; }
         if (INV) w.y = -w.y;
         r[j] = cmulf(r[j], w);
@@ -354,7 +355,7 @@ __device__ __forceinline__ void warp_fft(float2 (&r)[E], const float2 *__restric
     for (int s = 0; s < 5; ++s) {
         const int h = 16 >> s;
         const bool upper = (lane & h) != 0;
-        float2 w = tw[E * ((lane & (h - 1)) * (16 / h))];
+        float2 w = tw[S * E * ((lane & (h - 1)) * (16 / h))];
         if (INV) w.y = -w.y;
 #pragma unroll
         for (int j = 0; j < E; ++j) {
@@ -410,6 +411,7 @@ __device__ __forceinline__ void warp_dct2_real(const float *xm, float2 *zb, cons
     warp_fft<E, false>(r, twh, lane);
     warp_fft_store<E>(r, zb, lane);
     __syncwarp();
+#pragma unroll 4
     for (int k = lane; k <= H; k += 32) {
         const float2 zk = zb[swz(k & (H - 1))];
         float2 zc = zb[swz((H - k) & (H - 1))];
@@ -438,7 +440,7 @@ __device__ __forceinline__ void warp_inv_real(XFn x, bool sine, float2 *zb, cons
                                               const float2 *tw_n, const float2 *ek, int lane, Emit emit) {
     constexpr int H = 32 * E, N = 2 * H;
     float2 r[E];
-#pragma unroll 1
+#pragma unroll 4
     for (int t = 0; t < E; ++t) {
         const int k = lane + 32 * t;
         float2 v[2];
@@ -460,6 +462,7 @@ __device__ __forceinline__ void warp_inv_real(XFn x, bool sine, float2 *zb, cons
     warp_fft<E, true>(r, twh, lane);
     warp_fft_store<E>(r, zb, lane);
     __syncwarp();
+#pragma unroll 8
     for (int i = lane; i < N; i += 32) {
         const int p = (i & 1) ? (N - 1 - (i >> 1)) : (i >> 1);
         const float2 z = zb[swz(p >> 1)];
@@ -513,15 +516,17 @@ __global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
         }
         const unsigned long long *q_s = reinterpret_cast<const unsigned long long *>(wbase);
         float v[2 * E];
+        double ov4[4] = {0.0, 0.0, 0.0, 0.0};   // four independent FP64 chains
 #pragma unroll
         for (int t = 0; t < 2 * E; ++t) {
             const int i = lane + 32 * t;
             // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
             const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q_s[i]), fixed_inv), ini_s[i]);
             const float o = __fsub_rn(d, coef);
-            ovf += (double)(o > 0.0f ? o : 0.0f);    // src/epotential.rs:274-276
-            v[t] = __fmul_rn(d, inv_area);             // src/epotential.rs:284-285
+            ov4[t & 3] += (double)(o > 0.0f ? o : 0.0f);    // src/epotential.rs:274-276
+            v[t] = __fmul_rn(d, inv_area);                    // src/epotential.rs:284-285
         }
+        ovf = (ov4[0] + ov4[1]) + (ov4[2] + ov4[3]);
         if (zero_map) {
             ulonglong2 *zr = reinterpret_cast<ulonglong2 *>(dmap + (size_t)row * N);
 #pragma unroll
@@ -600,6 +605,7 @@ __global__ void __launch_bounds__(NW * 32) k_cols_w(
         warp_fft<E, false>(r, twh, lane);
         warp_fft_store<E>(r, zb, lane);
         __syncwarp();
+#pragma unroll 4
         for (int k = lane; k <= H; k += 32) {
             const float2 zk = zb[swz(k & (H - 1))];
             float2 zc = zb[swz((H - k) & (H - 1))];
@@ -671,6 +677,325 @@ __global__ void __launch_bounds__(NW * 32) k_rows_inv_w(
     __syncwarp();
     warp_inv_real<E>([&](int u) { return xb[u]; }, kind == 1, zb, tb.twh, tb.tw, tb.ek, lane,
                      [&](int i, float v) { out[i] = v; });
+}
+
+// ===================================================================
+// Group transforms: kQ = 4 warps per sequence (sides 512..2048).  At a 1024^2
+// grid there are only 1024 rows or columns, about seven per SM, so one warp
+// per sequence leaves the SMs latency bound; splitting each sequence over four
+// warps gives four times the warps, each with a quarter of the serial work.
+//
+// H-point FFT, H = M kQ, M = 32 E, by decimation in frequency: input index
+// n = n2 + M q, output index k = k1 + kQ k2 (q, k1 < kQ; n2, k2 < M):
+//   a_k1[n2]        = W_H^(n2 k1) sum_q W_kQ^(q k1) z[n2 + M q]   (any thread)
+//   Z[k1 + kQ k2]   = sum_n2 W_M^(n2 k2) a_k1[n2]                 (warp k1)
+// The first stage reads and writes consecutive elements across lanes; the only
+// strided access, the final scatter to natural order, goes through the XOR
+// swizzle xsw (two wavefronts per 64-bit warp access for E = 2, 4, 8).  The
+// group synchronises with a named barrier of its 128 threads (ids 1..).
+// ===================================================================
+constexpr int kQ = 4;
+
+__device__ __forceinline__ void group_bar(int id) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(kQ * 32) : "memory");
+}
+
+__device__ __forceinline__ int xsw(int f) { return f ^ ((f >> 5) & 15); }
+
+// W_H^idx, 0 <= idx < H, from the half table tw (k < H/2)
+template <int H>
+__device__ __forceinline__ float2 tw_full(const float2 *tw, int idx) {
+    float2 w = idx < H / 2 ? tw[idx] : tw[idx - H / 2];
+    if (idx >= H / 2) { w.x = -w.x; w.y = -w.y; }
+    return w;
+}
+
+// zin(n) gives z[n] (n < H); on exit xs[xsw(k)] = Z[k] for every k < H,
+// visible to the whole group.  ys, xs: H float2 each; twh: W_H^k, k < H/2.
+template <int E, bool INV, typename ZIn>
+__device__ __forceinline__ void group_fft(ZIn zin, const float2 *twh, float2 *ys, float2 *xs, int q, int lane,
+                                          int gt, int bar) {
+    constexpr int M = 32 * E, H = M * kQ;
+#pragma unroll
+    for (int n2 = gt; n2 < M; n2 += 32 * kQ) {
+        const float2 a0 = zin(n2), a1 = zin(n2 + M), a2 = zin(n2 + 2 * M), a3 = zin(n2 + 3 * M);
+        const float2 s0 = make_float2(a0.x + a2.x, a0.y + a2.y), s1 = make_float2(a0.x - a2.x, a0.y - a2.y);
+        const float2 s2 = make_float2(a1.x + a3.x, a1.y + a3.y), s3 = make_float2(a1.x - a3.x, a1.y - a3.y);
+        float2 x1, x3;
+        if (!INV) {   // W_4 = -i
+            x1 = make_float2(s1.x + s3.y, s1.y - s3.x);
+            x3 = make_float2(s1.x - s3.y, s1.y + s3.x);
+        } else {      // W_4 = +i
+            x1 = make_float2(s1.x - s3.y, s1.y + s3.x);
+            x3 = make_float2(s1.x + s3.y, s1.y - s3.x);
+        }
+        float2 w1 = tw_full<H>(twh, n2), w2 = tw_full<H>(twh, 2 * n2), w3 = tw_full<H>(twh, 3 * n2);
+        if (INV) { w1.y = -w1.y; w2.y = -w2.y; w3.y = -w3.y; }
+        ys[n2] = make_float2(s0.x + s2.x, s0.y + s2.y);
+        ys[M + n2] = cmulf(x1, w1);
+        ys[2 * M + n2] = cmulf(make_float2(s0.x - s2.x, s0.y - s2.y), w2);
+        ys[3 * M + n2] = cmulf(x3, w3);
+    }
+    group_bar(bar);
+    float2 r[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) r[j] = ys[q * M + lane + 32 * j];
+    warp_fft<E, INV, kQ>(r, twh, lane);
+    const int pl = (int)(__brev((unsigned)lane) >> 27);
+#pragma unroll
+    for (int j = 0; j < E; ++j) xs[xsw(q + kQ * (brev_c<E>(j) + E * pl))] = r[j];
+    group_bar(bar);
+}
+
+// DCT-II post-processing (as warp_dct2_real) from the group FFT of the
+// Makhoul-ordered row: emit(k, y[k]) for every k < N across the group.
+template <int H, typename Emit>
+__device__ __forceinline__ void group_dct2_post(const float2 *xs, const float2 *tw_n, const float2 *ek, int gt,
+                                                Emit emit) {
+    constexpr int N = 2 * H;
+#pragma unroll 2
+    for (int k = gt; k <= H; k += 32 * kQ) {
+        const float2 zk = xs[xsw(k & (H - 1))];
+        float2 zc = xs[xsw((H - k) & (H - 1))];
+        zc.y = -zc.y;
+        const float2 ev = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
+        const float2 od = make_float2(0.5f * (zk.y - zc.y), -0.5f * (zk.x - zc.x));
+        const float2 w = k < H ? tw_n[k] : make_float2(-1.0f, 0.0f);
+        const float2 v = make_float2(ev.x + (w.x * od.x - w.y * od.y), ev.y + (w.x * od.y + w.y * od.x));
+        const float2 e = ek[k];
+        emit(k, e.x * v.x - e.y * v.y);
+        if (k > 0 && k < H) {
+            const float2 e2 = ek[N - k];
+            emit(N - k, e2.x * v.x + e2.y * v.y);
+        }
+    }
+}
+
+// Inverse along one axis (as warp_inv_real) by a group: x(u) gives X[u]; the
+// folded Hermitian spectrum is formed inside the group FFT's first stage.
+template <int E, typename XFn, typename Emit>
+__device__ __forceinline__ void group_inv_real(XFn x, bool sine, float2 *ys, float2 *xs, const float2 *twh,
+                                               const float2 *tw_n, const float2 *ek, int q, int lane, int gt,
+                                               int bar, Emit emit) {
+    constexpr int H = 32 * E * kQ, N = 2 * H;
+    auto zin = [&](int k) -> float2 {
+        float2 v[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int u = k + h * H;
+            const int un = N - u;   // in (0, N]; X[N] := 0
+            const float xu = x(u);
+            const float xn = (un == N) ? 0.0f : x(un);
+            if (!sine) v[h] = idct_spec(xu, xn, ek[u]);
+            else v[h] = (u == 0) ? make_float2(0.f, 0.f) : idct_spec(xn, xu, ek[u]);
+        }
+        const float2 fe = make_float2(v[0].x + v[1].x, v[0].y + v[1].y);
+        const float2 d = make_float2(v[0].x - v[1].x, v[0].y - v[1].y);
+        const float2 w = tw_n[k];   // e^{-2 pi i k / N}; Fo = d * conj(w)
+        const float2 fo = make_float2(d.x * w.x + d.y * w.y, d.y * w.x - d.x * w.y);
+        return make_float2(fe.x - fo.y, fe.y + fo.x);
+    };
+    group_fft<E, true>(zin, twh, ys, xs, q, lane, gt, bar);
+#pragma unroll 4
+    for (int i = gt; i < N; i += 32 * kQ) {
+        const int p = (i & 1) ? (N - 1 - (i >> 1)) : (i >> 1);
+        const float2 z = xs[xsw(p >> 1)];
+        float val = (p & 1) ? z.y : z.x;
+        if (sine && (i & 1)) val = -val;
+        emit(i, val);
+    }
+}
+
+// R1 (group form): rows forward DCT-II, one group of four warps per row, G rows
+// per block.  Per group: [0, 2H) the row's int64 sums (bulk copy), later the
+// Makhoul staging xm in [0, H) and xs in [H, 2H); [2H, 3H) the row of the
+// initial map (bulk copy); [3H, 4H) ys.
+template <int E, int G>
+__global__ void __launch_bounds__(G * kQ * 32) k_rows_dct_g(
+    int m, const float2 *__restrict__ tw_n, const float2 *__restrict__ ek_n,
+    const float *__restrict__ rho_in, unsigned long long *__restrict__ dmap,
+    const float *__restrict__ initial, float fixed_inv, float coef, float inv_area, int zero_map,
+    float *__restrict__ rho_out, float *__restrict__ t1, double *__restrict__ partials,
+    DevState *__restrict__ st, double movable_area) {
+    constexpr int H = 32 * E * kQ, N = 2 * H, PT = N / (32 * kQ);   // values per thread
+    if (st && st->done) return;
+    extern __shared__ __align__(16) float2 sm[];
+    __shared__ __align__(8) uint64_t bar[G];
+    __shared__ double shr[G * kQ];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grp = warp / kQ, q = warp % kQ, gt = q * 32 + lane, gbar = 1 + grp;
+    const int row = blockIdx.x * G + grp;
+    float2 *gbase = sm + tables_f2<H>() + grp * 4 * H;
+    float *xm = reinterpret_cast<float *>(gbase);
+    float2 *xs = gbase + H;
+    float *ini_s = reinterpret_cast<float *>(gbase + 2 * H);
+    float2 *ys = gbase + 3 * H;
+    const bool from_map = rho_in == nullptr;
+    if (from_map && gt == 0) {
+        mbar_init(&bar[grp], 1);
+        mbar_expect_tx(&bar[grp], 12u * N);
+        bulk_load(gbase, dmap + (size_t)row * N, 8u * N, &bar[grp]);
+        bulk_load(ini_s, initial + (size_t)row * N, 4u * N, &bar[grp]);
+    }
+    const AxisTables tb = load_tables<G * kQ, H>(sm, tw_n, ek_n);
+    __syncthreads();   // tables; the group's barrier initialisation
+    double ovf = 0.0;
+    float v[PT];
+    if (from_map) {
+        if (!mbar_wait(&bar[grp], 0)) {
+            if (gt == 0 && st) {
+                atomicOr(&st->status, kStatusWaitTimeout);
+                st->done = 1;
+            }
+            mbar_wait(&bar[grp], 0);   // the copy must land before the area is reused
+        }
+        const unsigned long long *q_s = reinterpret_cast<const unsigned long long *>(gbase);
+        double ov2[2] = {0.0, 0.0};
+#pragma unroll
+        for (int t = 0; t < PT; ++t) {
+            const int i = gt + 32 * kQ * t;
+            // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
+            const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q_s[i]), fixed_inv), ini_s[i]);
+            const float o = __fsub_rn(d, coef);
+            ov2[t & 1] += (double)(o > 0.0f ? o : 0.0f);   // src/epotential.rs:274-276
+            v[t] = __fmul_rn(d, inv_area);                   // src/epotential.rs:284-285
+        }
+        ovf = ov2[0] + ov2[1];
+        if (zero_map) {
+            ulonglong2 *zr = reinterpret_cast<ulonglong2 *>(dmap + (size_t)row * N);
+#pragma unroll
+            for (int k = 0; k < N / (64 * kQ); ++k) zr[gt + 32 * kQ * k] = make_ulonglong2(0ull, 0ull);
+        }
+        if (rho_out) {
+#pragma unroll
+            for (int t = 0; t < PT; ++t) rho_out[(size_t)row * N + gt + 32 * kQ * t] = v[t];
+        }
+    } else {
+#pragma unroll
+        for (int t = 0; t < PT; ++t) v[t] = rho_in[(size_t)row * N + gt + 32 * kQ * t];
+    }
+    group_bar(gbar);   // the staged row is consumed: xm may overwrite it
+#pragma unroll
+    for (int t = 0; t < PT; ++t) {
+        const int i = gt + 32 * kQ * t;
+        xm[makhoul_pos(i, N)] = v[t];
+    }
+    group_bar(gbar);
+    const float2 *xm2 = reinterpret_cast<const float2 *>(xm);
+    group_fft<E, false>([&](int i) { return xm2[i]; }, tb.twh, ys, xs, q, lane, gt, gbar);
+    float *out = t1 + (size_t)row * N;
+    group_dct2_post<H>(xs, tb.tw, tb.ek, gt, [&](int k, float y) { out[k] = y; });
+    if (from_map && partials) {
+        const double b = block_sum(ovf, shr);
+        double vals[1] = {b};
+        if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_OVF], gridDim.x)) {
+            const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
+            if (threadIdx.x == 0) {
+                st->overflow = tot;
+                st->overflow_f = (float)(tot / movable_area);
+                st->ctr[CTR_OVF] = 0;
+            }
+        }
+    }
+}
+
+// C1 (group form): G columns per block, one group per column.  Coalesced tile
+// load, forward DCT-II along x into A (shared), 1/(wu^2+wv^2) per bin, then for
+// each output kind the weighted inverse along x and a coalesced tile store.
+// Per group: ab [0, H) (Makhoul staging, then A, as floats), ib [H, 2H) (floats),
+// ys [2H, 3H), xs [3H, 4H).
+template <int E, int G>
+__global__ void __launch_bounds__(G * kQ * 32) k_cols_g(
+    int n, const float2 *__restrict__ tw_m, const float2 *__restrict__ ek_m,
+    const float *__restrict__ wu_g, const float *__restrict__ wv, const float *__restrict__ t1,
+    float *__restrict__ tx, float *__restrict__ ty, float *__restrict__ tp, float scale4,
+    const DevState *__restrict__ st) {
+    constexpr int H = 32 * E * kQ, M = 2 * H, S = G + 1;   // tile row stride (odd)
+    if (st && st->done) return;
+    extern __shared__ __align__(16) float2 sm[];
+    const AxisTables tb = load_tables<G * kQ, H>(sm, tw_m, ek_m);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grp = warp / kQ, q = warp % kQ, gt = q * 32 + lane, gbar = 1 + grp;
+    float2 *gbase = sm + tables_f2<H>() + grp * 4 * H;
+    float *ab = reinterpret_cast<float *>(gbase);
+    float *ib = reinterpret_cast<float *>(gbase + H);
+    float2 *ys = gbase + 2 * H, *xs = gbase + 3 * H;
+    float *wu = reinterpret_cast<float *>(sm + tables_f2<H>() + G * 4 * H);
+    float *tile = wu + M;
+    const int j0 = blockIdx.x * G;
+    for (int k = threadIdx.x; k < M; k += blockDim.x) wu[k] = wu_g[k];
+    for (int idx = threadIdx.x; idx < M * G; idx += blockDim.x) {
+        const int i = idx / G, c = idx - i * G;
+        tile[i * S + c] = t1[(size_t)i * n + j0 + c];
+    }
+    __syncthreads();
+    const int j = j0 + grp;
+    for (int i = gt; i < M; i += 32 * kQ) ab[makhoul_pos(i, M)] = tile[i * S + grp];
+    group_bar(gbar);
+    {
+        const float2 *ab2 = reinterpret_cast<const float2 *>(ab);
+        group_fft<E, false>([&](int i) { return ab2[i]; }, tb.twh, ys, xs, q, lane, gt, gbar);   // ab's staging is consumed
+        group_dct2_post<H>(xs, tb.tw, tb.ek, gt, [&](int k, float y) {
+            ab[k] = scale4 * y;
+            ib[k] = inv_k2(k, j, wu, wv);
+        });
+        group_bar(gbar);
+    }
+    const float wvj = wv[j];
+    const int nkinds = tp ? 3 : 2;
+#pragma unroll 1
+    for (int kind = 0; kind < nkinds; ++kind) {
+        // kind 0: field_x  IDXST_x of A * wu / 2k^2   (src/idxst_idct.rs, src/frequencies.rs:52-58)
+        // kind 1: field_y  IDCT_x  of A * wv / 2k^2   (src/idct_idxst.rs, src/frequencies.rs:60-66)
+        // kind 2: potential IDCT_x of A / k^2          (src/idct2.rs)
+        auto xfn = [&](int u) -> float {
+            const float iv = ib[u];
+            float wgt;
+            if (kind == 0) wgt = __fmul_rn(__fmul_rn(wu[u], iv), 0.5f);
+            else if (kind == 1) wgt = __fmul_rn(__fmul_rn(wvj, iv), 0.5f);
+            else wgt = iv;
+            return __fmul_rn(ab[u], wgt);
+        };
+        group_inv_real<E>(xfn, kind == 0, ys, xs, tb.twh, tb.tw, tb.ek, q, lane, gt, gbar,
+                          [&](int i, float v) { tile[i * S + grp] = v; });
+        __syncthreads();
+        float *out = kind == 0 ? tx : (kind == 1 ? ty : tp);
+        for (int idx = threadIdx.x; idx < M * G; idx += blockDim.x) {
+            const int i = idx / G, c = idx - i * G;
+            out[(size_t)i * n + j0 + c] = tile[i * S + c];
+        }
+        __syncthreads();
+    }
+}
+
+// R2 (group form): rows inverse along y, one group per (row, output kind), G
+// tasks per block.  Per group: xb [0, H) (the input row as floats; later xs),
+// ys [H, 2H).
+template <int E, int G>
+__global__ void __launch_bounds__(G * kQ * 32) k_rows_inv_g(
+    int m, int nkinds, const float2 *__restrict__ tw_n, const float2 *__restrict__ ek_n,
+    const float *__restrict__ tx, const float *__restrict__ ty, const float *__restrict__ tp,
+    float *__restrict__ fx, float *__restrict__ fy, float *__restrict__ psi,
+    const DevState *__restrict__ st) {
+    constexpr int H = 32 * E * kQ, N = 2 * H;
+    if (st && st->done) return;
+    extern __shared__ __align__(16) float2 sm[];
+    const AxisTables tb = load_tables<G * kQ, H>(sm, tw_n, ek_n);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grp = warp / kQ, q = warp % kQ, gt = q * 32 + lane, gbar = 1 + grp;
+    float2 *gbase = sm + tables_f2<H>() + grp * 2 * H;
+    float *xb = reinterpret_cast<float *>(gbase);
+    float2 *xs = gbase, *ys = gbase + H;   // xs reuses xb once the spectrum is folded
+    const int task = blockIdx.x * G + grp;
+    const int row = task / nkinds, kind = task - row * nkinds;
+    // kind 0: field_x = IDCT_y(tx); kind 1: field_y = IDXST_y(ty); kind 2: psi = IDCT_y(tp)
+    const float *in = (kind == 0 ? tx : (kind == 1 ? ty : tp)) + (size_t)row * N;
+    float *out = (kind == 0 ? fx : (kind == 1 ? fy : psi)) + (size_t)row * N;
+#pragma unroll
+    for (int t = 0; t < N / (32 * kQ); ++t) xb[gt + 32 * kQ * t] = in[gt + 32 * kQ * t];
+    __syncthreads();   // tables and the staged rows
+    group_inv_real<E>([&](int u) { return xb[u]; }, kind == 1, ys, xs, tb.twh, tb.tw, tb.ek, q, lane, gt,
+                      gbar, [&](int i, float v) { out[i] = v; });
 }
 
 int ilog2(int v) {
@@ -751,6 +1076,54 @@ static cudaError_t prepare_w() {
     return e;
 }
 
+// group kernels: sides 512..2048 (E = side / 256), G sequences per block
+constexpr int kRowGroups = 2, kColGroups = 4, kInvGroups = 4;
+static bool group_side(int v) { return v >= 512 && v <= 2048; }
+template <int E>
+static size_t rows_dct_g_smem() { return sizeof(float2) * (size_t)(tables_f2<128 * E>() + kRowGroups * 4 * 128 * E); }
+template <int E>
+static size_t cols_g_smem() {
+    return sizeof(float2) * (size_t)(tables_f2<128 * E>() + kColGroups * 4 * 128 * E) +
+           sizeof(float) * (size_t)(256 * E) * (kColGroups + 2);
+}
+template <int E>
+static size_t rows_inv_g_smem() { return sizeof(float2) * (size_t)(tables_f2<128 * E>() + kInvGroups * 2 * 128 * E); }
+template <int E>
+static cudaError_t prepare_g() {
+    cudaError_t e = cudaFuncSetAttribute(k_rows_dct_g<E, kRowGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)rows_dct_g_smem<E>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_cols_g<E, kColGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)cols_g_smem<E>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_rows_inv_g<E, kInvGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)rows_inv_g_smem<E>());
+    return e;
+}
+template <int E>
+static void rows_dct_g(const SpectralPlan &p, const SpectralArgs &a, bool from_map) {
+    k_rows_dct_g<E, kRowGroups><<<p.m / kRowGroups, kRowGroups * kQ * 32, rows_dct_g_smem<E>(), p.stream>>>(
+        p.m, p.tw_n, p.ek_n, a.rho_in, a.dmap, a.initial, a.fixed_inv, a.coef, a.inv_bin_area,
+        a.zero_map ? 1 : 0, a.rho_out, p.t1, from_map ? a.partials : nullptr, a.st, a.movable_area);
+}
+template <int E>
+static void cols_g(const SpectralPlan &p, const SpectralArgs &a, float scale4, float *tp) {
+    k_cols_g<E, kColGroups><<<p.n / kColGroups, kColGroups * kQ * 32, cols_g_smem<E>(), p.stream>>>(
+        p.n, p.tw_m, p.ek_m, p.wu, p.wv, p.t1, p.tx, p.ty, tp, scale4, a.st);
+}
+template <int E>
+static void rows_inv_g(const SpectralPlan &p, const SpectralArgs &a, float *tp) {
+    const int nk = tp ? 3 : 2;
+    k_rows_inv_g<E, kInvGroups><<<p.m * nk / kInvGroups, kInvGroups * kQ * 32, rows_inv_g_smem<E>(), p.stream>>>(
+        p.m, nk, p.tw_n, p.ek_n, p.tx, p.ty, tp, a.fx, a.fy, a.psi, a.st);
+}
+#define ERP_DISPATCH_G(side, FN, ...)           \
+    switch (side) {                             \
+    case 512: FN<2>(__VA_ARGS__); break;        \
+    case 1024: FN<4>(__VA_ARGS__); break;       \
+    default: FN<8>(__VA_ARGS__); break;         \
+    }
+
 // Opt the spectral kernels into large dynamic shared memory on the current device.
 cudaError_t spectral_prepare() {
     cudaError_t e = cudaFuncSetAttribute(k_rows_dct<kRowPairs>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -763,6 +1136,9 @@ cudaError_t spectral_prepare() {
     if (e == cudaSuccess) e = prepare_w<8>();
     if (e == cudaSuccess) e = prepare_w<16>();
     if (e == cudaSuccess) e = prepare_w<32>();
+    if (e == cudaSuccess) e = prepare_g<2>();
+    if (e == cudaSuccess) e = prepare_g<4>();
+    if (e == cudaSuccess) e = prepare_g<8>();
     return e;
 }
 
@@ -772,6 +1148,7 @@ size_t spectral_smem_bytes(int m, int n) {
 }
 
 static bool warp_side(int v) { return v >= 64 && v <= 2048; }
+
 
 template <int E>
 static void rows_dct_w(const SpectralPlan &p, const SpectralArgs &a, bool from_map) {
@@ -805,7 +1182,9 @@ void launch_spectral_plan(const SpectralPlan &p, const SpectralArgs &a) {
     const int m = p.m, n = p.n;
     const bool from_map = a.rho_in == nullptr;
     const int rb = m / (2 * kRowPairs);
-    if (warp_side(n)) {
+    if (group_side(n)) {
+        ERP_DISPATCH_G(n, rows_dct_g, p, a, from_map);
+    } else if (warp_side(n)) {
         ERP_DISPATCH_E(n, rows_dct_w, p, a, from_map);
     } else {
         k_rows_dct<kRowPairs><<<rb, kThreads, rows_smem(n, kRowPairs), p.stream>>>(
@@ -815,7 +1194,9 @@ void launch_spectral_plan(const SpectralPlan &p, const SpectralArgs &a) {
     }
     const float scale4 = 4.0f / (float)((double)m * (double)n);
     float *tp = a.psi ? p.tp : nullptr;
-    if (warp_side(m)) {
+    if (group_side(m)) {
+        ERP_DISPATCH_G(m, cols_g, p, a, scale4, tp);
+    } else if (warp_side(m)) {
         ERP_DISPATCH_E(m, cols_w, p, a, scale4, tp);
     } else if (col_pairs(m) == 4) {
         k_cols<4><<<n / 8, kThreads, cols_smem(m, 4), p.stream>>>(m, n, p.logm, p.tw_m, p.ek_m, p.wu,
@@ -826,7 +1207,9 @@ void launch_spectral_plan(const SpectralPlan &p, const SpectralArgs &a) {
                                                                   p.wv, p.t1, p.tx, p.ty, tp, scale4,
                                                                   a.st);
     }
-    if (warp_side(n)) {
+    if (group_side(n)) {
+        ERP_DISPATCH_G(n, rows_inv_g, p, a, tp);
+    } else if (warp_side(n)) {
         ERP_DISPATCH_E(n, rows_inv_w, p, a, tp);
     } else {
         k_rows_inv<kRowPairs><<<rb, kThreads, rows_smem(n, kRowPairs), p.stream>>>(

@@ -48,6 +48,9 @@ DESIGNS = {
     "edge_16x64": (lambda: edge_design(seed=9), 16, 64),
     "synth3k_64": (lambda: small_synth(3000, seed=11), 64, 64),
     "synth20k_256": (lambda: small_synth(20000, seed=1, macros=0, io=400), 256, 256),
+    # four-warp transform paths from the fixed-point map (rows 512 / 2048, columns 1024)
+    "synth60k_1024x512": (lambda: small_synth(60000, seed=3), 1024, 512),
+    "synth20k_256x2048": (lambda: small_synth(20000, seed=4, macros=2, io=200), 256, 2048),
 }
 
 
@@ -199,10 +202,11 @@ def test_run_retires_at_overflow(R):
 
 
 @pytest.mark.parametrize("m,n", [(32, 1024), (1024, 32), (2048, 64), (16, 256), (128, 128),
-                                 (1024, 1024)])
+                                 (1024, 1024), (512, 2048), (2048, 512)])
 def test_spectral_standalone_shapes(R, O, m, n):
-    """Every transform-size path (warp FFT for 32..1024, shared-memory FFT
-    otherwise) against the FP32 oracle pipeline."""
+    """Every transform-size path (four-warp FFT for sides 512..2048, one-warp FFT
+    for 64..256, shared-memory radix-2 FFT otherwise) against the FP32 oracle
+    pipeline."""
     import torch
     rng = np.random.default_rng(m * 7 + n)
     rho = (0.5 + rng.random((m, n))).astype(np.float32)
