@@ -30,18 +30,25 @@ L2_BYTES = 129 * 2 ** 20
 
 # Algorithmic bytes per launch of each stage (FP32 = 4 B, index = 4 B,
 # int64 = 8 B; each array counted once): N movable cells, P pins, E nets,
-# B = m*n bins.
+# B = m*n bins.  wirelength (k_wa): per pin the cell index (4), the pin offset
+# (8), the gathered (x, y) (8) and the pin gradient written (8); per net its
+# HPWL (4) (the net_ptr reads of the ~1 % of nets above 8 pins are left out).
+# wl_gather: per pin its slot index (4) and gradient (8); per cell the range
+# (4) and the gradient pair written (8).
 ALG_BYTES = {
-    "wirelength": lambda N, P, E, B: 40 * P + 4 * E + 20 * N,
+    "wirelength": lambda N, P, E, B: 28 * P + 4 * E,
+    "wl_gather": lambda N, P, E, B: 12 * P + 12 * N,
     "density": lambda N, P, E, B: 28 * N + 8 * B,
     "spectral": lambda N, P, E, B: 12 * B + 12 * B,
     "force": lambda N, P, E, B: 36 * N + 8 * B,
     "nesterov": lambda N, P, E, B: 76 * N,
     "scheduler": lambda N, P, E, B: 0,
 }
-# DRAM bytes per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum),
-# filled from the committed profiles/ summaries; None until captured.
-NCU_TRAFFIC = {}
+# DRAM bytes per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum)
+# of one --set full capture of the kernel on this workload (cold L2, the
+# profiler's default cache control); the command and figures are in
+# profiles/k_wa_1M_cells.md.
+NCU_TRAFFIC = {("large", "wirelength"): 69.092352e6 + 13.533184e6}
 
 
 def measured_peak_gbs():

@@ -275,13 +275,14 @@ erp_status erp_estimate_footprint(const erp_design *design, const erp_params *pa
  * Mutates the placement state (positions, scheduler): call it after the
  * measured run. */
 typedef enum erp_stage {
-    ERP_STAGE_WIRELENGTH = 0, /* WA nets + HPWL reduction + instance gather */
-    ERP_STAGE_DENSITY = 1,    /* map clear + density scatter */
-    ERP_STAGE_SPECTRAL = 2,   /* map conversion + overflow + Poisson solve (3 passes) */
-    ERP_STAGE_FORCE = 3,      /* electric force gather */
-    ERP_STAGE_NESTEROV = 4,   /* rescale + preconditioned gradient / Lipschitz + update */
-    ERP_STAGE_SCHEDULER = 5,
-    ERP_NUM_STAGES = 6
+    ERP_STAGE_WIRELENGTH = 0, /* WA nets + HPWL reduction (pin gradients) */
+    ERP_STAGE_WL_GATHER = 1,  /* instance gradients from the pin gradients */
+    ERP_STAGE_DENSITY = 2,    /* map clear + density scatter */
+    ERP_STAGE_SPECTRAL = 3,   /* map conversion + overflow + Poisson solve (3 passes) */
+    ERP_STAGE_FORCE = 4,      /* electric force gather */
+    ERP_STAGE_NESTEROV = 5,   /* rescale + preconditioned gradient / Lipschitz + update */
+    ERP_STAGE_SCHEDULER = 6,
+    ERP_NUM_STAGES = 7
 } erp_stage;
 erp_status erp_profile_stages(erp_ctx *ctx, int32_t reps, float *ms_out);
 

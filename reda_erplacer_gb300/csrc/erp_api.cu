@@ -799,7 +799,8 @@ extern "C" erp_status erp_profile_stages(erp_ctx *ctx, int32_t reps, float *ms_o
             cudaMemsetAsync(flush, r & 0xff, flush_bytes, c.stream);
             cudaEventRecord(e0, c.stream);
             switch (stage) {
-            case ERP_STAGE_WIRELENGTH: launch_wirelength(c, -1.0f); launch_wl_gather(c); break;
+            case ERP_STAGE_WIRELENGTH: launch_wirelength(c, -1.0f); break;
+            case ERP_STAGE_WL_GATHER: launch_wl_gather(c); break;
             case ERP_STAGE_DENSITY:
                 cudaMemsetAsync(c.dmap, 0, sizeof(unsigned long long) * mn, c.stream);
                 launch_density_scatter(c);
