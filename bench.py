@@ -216,6 +216,116 @@ def batch_section(args, device):
     }
 
 
+def poisson_fp64(rho, bw, bh):
+    """FP64 closed form of the Poisson solve (the per-axis transforms of the
+    reference pipelines): A = (2/m)(2/n) DCT-II_m DCT-II_n(rho);
+    field_x = IDXST_m IDCT_n(A wu / 2k^2), field_y = IDCT_m IDXST_n(A wv / 2k^2),
+    psi = IDCT_m IDCT_n(A / k^2), k^2 = wu^2 + wv^2, [0,0] -> 0."""
+    import numpy as np
+    from scipy.fft import dct
+    m, n = rho.shape
+    a = dct(dct(rho.astype(np.float64), type=2, axis=0), type=2, axis=1) / (m * n)
+    wu = 2.0 * np.pi * np.arange(m) / m
+    wv = 2.0 * np.pi * np.arange(n) / n * (bw / bh)
+    k2 = wu[:, None] ** 2 + wv[None, :] ** 2
+    k2[0, 0] = 1.0
+    inv = 1.0 / k2
+    inv[0, 0] = 0.0
+
+    def idct(x, ax):   # y_i = X_0 + 2 sum_{u>=1} X_u cos(pi u (2i+1) / 2N)
+        return dct(x, type=3, axis=ax)
+
+    def idxst(x, ax):  # y_i = (-1)^i IDCT(X')_i, X'_0 = 0, X'_u = X_(N-u)
+        xp = np.zeros_like(x)
+        if ax == 0:
+            xp[1:] = x[1:][::-1]
+        else:
+            xp[:, 1:] = x[:, 1:][:, ::-1]
+        y = idct(xp, ax)
+        sgn = np.where(np.arange(x.shape[ax]) % 2 == 0, 1.0, -1.0)
+        return y * (sgn[:, None] if ax == 0 else sgn[None, :])
+
+    fx = idxst(idct(a * (0.5 * wu[:, None] * inv), 1), 0)
+    fy = idct(idxst(a * (0.5 * wv[None, :] * inv), 1), 0)
+    psi = idct(idct(a * inv, 1), 0)
+    return fx, fy, psi
+
+
+def spectral_section(args, device):
+    """Isolated Poisson solve on the seeded density maps (0.7 background, 2,000
+    Gaussian blobs, 10 macro blocks) at 512^2, 1024^2 and 2048^2 bins: FP32 FFT
+    path, time per solve (CUDA events, L2 flushed before each solve), the
+    roofline on 16 B per bin (rho in; field_x, field_y, psi out) and the relative
+    L2 error of each output against the FP64 closed form."""
+    import numpy as np
+    import torch
+    import reda_erplacer_gb300 as R
+    peak, peak_kind = measured_peak_gbs()
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device=f"cuda:{device}")
+    out = {}
+    for side in (512, 1024, 2048):
+        rho = R.workload_spectral(side, seed=3000 + side)
+        ref = poisson_fp64(rho, 1.0, 1.0)
+        s = torch.cuda.Stream(device=device)
+        sol = R.SpectralSolver(side, side, 1.0, 1.0, stream=s.cuda_stream)
+        r = torch.tensor(rho, device=f"cuda:{device}")
+        outs = [torch.empty_like(r) for _ in range(3)]
+        ptrs = [t.data_ptr() for t in outs]
+        with torch.cuda.stream(s):
+            for _ in range(3):
+                sol.solve(r.data_ptr(), *ptrs)
+            ts = []
+            for _ in range(args.spectral_reps):
+                flush.fill_(1.0)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                sol.solve(r.data_ptr(), *ptrs)
+                e1.record(s)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        got = [t.cpu().numpy().astype(np.float64) for t in outs]
+        err = [float(np.linalg.norm(g - w) / np.linalg.norm(w)) for g, w in zip(got, ref)]
+        us = 1000.0 * float(np.median(ts))
+        achieved = 16.0 * side * side / (us * 1e-6) / 1e9
+        out[f"{side}x{side}"] = {
+            "fp32_fft": {"us_per_solve": us, "achieved_gbs": achieved, "frac": achieved / peak,
+                         "peak_kind": peak_kind, "err_field_x": err[0], "err_field_y": err[1],
+                         "err_potential": err[2]},
+            "tf32_dct_gemm": "not built", "bf16x3_dct_gemm": "not built"}
+        sol.close()
+    return out
+
+
+class LazyJobs:
+    """The serving stream's jobs, generated on a thread pool just ahead of use
+    (at most `ahead` outstanding); the server copies a design when it is
+    submitted, so each one is dropped once taken."""
+
+    def __init__(self, specs, ahead=256):
+        from concurrent.futures import ThreadPoolExecutor
+        import reda_erplacer_gb300 as R
+        self.make = R.design.batch_job
+        self.specs = specs
+        self.ex = ThreadPoolExecutor(max(1, os.cpu_count() or 1))
+        self.fut = {}
+        self.next = 0
+        self.ahead = ahead
+
+    def __len__(self):
+        return len(self.specs)
+
+    def __getitem__(self, i):
+        while self.next < len(self.specs) and self.next <= i + self.ahead:
+            self.fut[self.next] = self.ex.submit(self.make, *self.specs[self.next])
+            self.next += 1
+        return self.fut.pop(i).result()
+
+    def close(self):
+        self.ex.shutdown(wait=False, cancel_futures=True)
+
+
 def serve_section(args, device):
     """Serving workload: an open-loop stream of jobs (cells log-uniform 5k-500k,
     each its own seed) with Poisson arrivals at 80 % of the capacity measured by
@@ -226,23 +336,26 @@ def serve_section(args, device):
     import numpy as np
     import reda_erplacer_gb300 as R
     from reda_erplacer_gb300.serving import Server, run_stream
-    mix = R.workload_batch(count=args.serve_jobs, seed=9000, min_cells=5000, max_cells=500000)
-    pilot = mix[: min(32, len(mix))]
+    specs = R.design.batch_specs(count=args.serve_jobs, seed=9000, min_cells=5000, max_cells=500000)
+    pilot = [R.design.batch_job(*sp) for sp in specs[: min(32, len(specs))]]
     bt = R.Batch([d for d, _ in pilot], [b for _, b in pilot], 1.0, start_mode=1, device=device)
     t0 = time.perf_counter()
     bt.run(args.batch_iters, stop_overflow=0.10)
     cap = len(pilot) / (time.perf_counter() - t0)
     bt.close()
+    del pilot
     rate = 0.8 * cap
     rng = np.random.default_rng(17)
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(mix)))
-    out = {"jobs": len(mix), "capacity_jobs_per_s": cap, "arrival_rate_jobs_per_s": rate,
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(specs)))
+    out = {"jobs": len(specs), "capacity_jobs_per_s": cap, "arrival_rate_jobs_per_s": rate,
            "hbm_budget_gb": 150.0, "max_iterations": args.batch_iters, "stop_overflow": 0.10}
     for name, max_active in (("continuous_batching", 64), ("one_at_a_time", 1)):
+        jobs = LazyJobs(specs)
         sv = Server(max_active=max_active, hbm_budget_gb=150.0, max_iterations=args.batch_iters,
                     stop_overflow=0.10, chunk=8, device=device)
-        res = run_stream(sv, mix, arrivals)
+        res = run_stream(sv, jobs, arrivals)
         sv.close()
+        jobs.close()
         lat = np.array([r["latency_s"] for r in res])
         span = max(r["finish_s"] for r in res) - min(r["submit_s"] for r in res)
         out[name] = {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
@@ -391,7 +504,9 @@ def run_ours(args):
     }
     if args.batch_count > 0:
         line["batched"] = batch_section(args, local)
-    if args.serve:
+    if not args.no_spectral:
+        line["spectral_solve"] = spectral_section(args, local)
+    if args.serve_jobs > 0:
         line["serving"] = serve_section(args, local)
     if rank == 0 and world == 1 and not args.no_cpu:
         v, dt = cpu_sample(d, cfg, args.cpu_iters, literal=False)
@@ -417,9 +532,10 @@ def main():
     ap.add_argument("--quick", action="store_true", help="timed steps only (for profiler runs)")
     ap.add_argument("--batch-count", type=int, default=64, help="instances of the batched section (0: skip)")
     ap.add_argument("--batch-iters", type=int, default=600)
-    ap.add_argument("--serve", action="store_true", help="also run the serving stream")
     ap.add_argument("--no-tto", action="store_true", help="skip the time-to-overflow-0.10 run")
-    ap.add_argument("--serve-jobs", type=int, default=200)
+    ap.add_argument("--no-spectral", action="store_true", help="skip the isolated-solve section")
+    ap.add_argument("--spectral-reps", type=int, default=20)
+    ap.add_argument("--serve-jobs", type=int, default=2000, help="jobs of the serving stream (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -4,10 +4,12 @@ include/erplacer.h.  All compute runs in liberplacer_gb300.so; importing this
 package fails if the library has not been built (no fallback)."""
 from . import lib
 from .lib import ErpError
-from .design import Design, synth, workload_small, workload_large, workload_batch, bins_for_cells
+from .design import (Design, bins_for_cells, synth, workload_batch, workload_large, workload_small,
+                     workload_spectral)
 from .placement import Batch, Placement, SpectralSolver
 
 lib.load()
 
-__all__ = ["Design", "synth", "workload_small", "workload_large", "workload_batch", "bins_for_cells",
+__all__ = ["Design", "synth", "workload_small", "workload_large", "workload_batch", "workload_spectral",
+           "bins_for_cells",
            "Placement", "Batch", "SpectralSolver", "ErpError"]

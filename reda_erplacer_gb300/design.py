@@ -116,20 +116,57 @@ def workload_large(seed=2):
         dict(bins=(1024, 1024), target_density=1.0, iterations=1000)
 
 
-def workload_batch(count=64, seed=4000, min_cells=2000, max_cells=200000):
-    """Instance mix of the batched workload: cells log-uniform in [min, max], nets
-    1.05 x cells, macros uniform 0-16, bin grid = power of two nearest
-    sqrt(cells)/2 clamped to 64..1024; each instance its own seed."""
+def batch_specs(count=64, seed=4000, min_cells=2000, max_cells=200000):
+    """Per-instance (cells, macros, seed) of the batched / served mix: cells
+    log-uniform in [min, max], macros uniform 0-16, each instance its own seed."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(count):
         cells = int(round(np.exp(rng.uniform(np.log(min_cells), np.log(max_cells)))))
         macros = int(rng.integers(0, 17))
-        d = synth(cells, int(round(1.05 * cells)), num_io=max(4, cells // 250), num_macros=macros,
-                  macro_area_frac=0.015, utilization=0.65, seed=seed + 1 + i)
-        b = bins_for_cells(cells)
-        out.append((d, (b, b)))
+        out.append((cells, macros, seed + 1 + i))
     return out
+
+
+def batch_job(cells, macros, seed):
+    """One instance of the mix: nets 1.05 x cells, bin grid = power of two nearest
+    sqrt(cells)/2 clamped to 64..1024."""
+    d = synth(cells, int(round(1.05 * cells)), num_io=max(4, cells // 250), num_macros=macros,
+              macro_area_frac=0.015, utilization=0.65, seed=seed)
+    b = bins_for_cells(cells)
+    return d, (b, b)
+
+
+def workload_batch(count=64, seed=4000, min_cells=2000, max_cells=200000):
+    """Instance mix of the batched workload (batch_specs, batch_job)."""
+    return [batch_job(*sp) for sp in batch_specs(count, seed, min_cells, max_cells)]
+
+
+def workload_spectral(side, seed=7):
+    """Density map of the isolated-solve workload: a uniform 0.7 background plus
+    2,000 Gaussian blobs (amplitude uniform 0.1-0.5, sigma uniform 1-20 bins,
+    centres uniform; each evaluated within 4 sigma) plus 10 rectangular macro
+    blocks (sides uniform side/32..side/8) set to 1.0.  float32 [side, side]."""
+    rng = np.random.default_rng(seed)
+    rho = np.full((side, side), 0.7, np.float64)
+    amp = rng.uniform(0.1, 0.5, 2000)
+    sig = rng.uniform(1.0, 20.0, 2000)
+    cx = rng.uniform(0, side, 2000)
+    cy = rng.uniform(0, side, 2000)
+    for a, s_, x0, y0 in zip(amp, sig, cx, cy):
+        r = int(np.ceil(4 * s_))
+        i0, i1 = max(0, int(x0) - r), min(side, int(x0) + r + 1)
+        j0, j1 = max(0, int(y0) - r), min(side, int(y0) + r + 1)
+        xi = (np.arange(i0, i1) + 0.5 - x0)[:, None]
+        yj = (np.arange(j0, j1) + 0.5 - y0)[None, :]
+        rho[i0:i1, j0:j1] += a * np.exp(-(xi * xi + yj * yj) / (2 * s_ * s_))
+    for _ in range(10):
+        w = int(rng.integers(side // 32, side // 8 + 1))
+        h = int(rng.integers(side // 32, side // 8 + 1))
+        x0 = int(rng.integers(0, side - w + 1))
+        y0 = int(rng.integers(0, side - h + 1))
+        rho[x0:x0 + w, y0:y0 + h] = 1.0
+    return rho.astype(np.float32)
 
 
 def bins_for_cells(num_cells):

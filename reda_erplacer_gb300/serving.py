@@ -6,8 +6,6 @@ import time
 import numpy as np
 
 from . import lib as L
-
-
 from .lib import JobResult, ServerParams
 
 
@@ -92,7 +90,9 @@ def run_stream(server, jobs, arrivals):
         now = server.now() - t_start
         while nxt < len(order) and arrivals[order[nxt]] <= now:
             i = int(order[nxt])
-            server.submit(i, jobs[i][0], jobs[i][1])
+            design, bins = jobs[i]   # fetched once (jobs may be generated lazily)
+            server.submit(i, design, bins)
+            del design
             nxt += 1
         active, queued = server.pump()
         results.extend(server.poll())

@@ -1,0 +1,34 @@
+"""The bench's FP64 closed-form Poisson solve (the reference for the
+isolated-solve errors) agrees with the oracle's FP64 solve to rounding, and the
+isolated-solve density map has the stated composition."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+@pytest.mark.parametrize("m,n,bw,bh", [(32, 64, 1.0, 1.0), (64, 32, 0.9, 1.7), (128, 128, 1.3, 1.1)])
+def test_fp64_closed_form_matches_oracle(built, m, n, bw, bh):
+    pytest.importorskip("scipy")
+    import bench
+    from oracle import erp_oracle as O
+    rng = np.random.default_rng(m + 3 * n)
+    rho = (0.5 + rng.random((m, n))).astype(np.float32)
+    got = bench.poisson_fp64(rho, bw, bh)
+    want = O.poisson(rho, bw, bh, dtype=np.float64)
+    for g, w in zip(got, want):
+        assert np.linalg.norm(g - w) / np.linalg.norm(w) < 1e-12
+
+
+def test_spectral_workload_map(built):
+    import reda_erplacer_gb300 as R
+    a = R.workload_spectral(512, seed=5)
+    b = R.workload_spectral(512, seed=5)
+    assert a.dtype == np.float32 and a.shape == (512, 512)
+    assert np.array_equal(a, b)                      # seeded
+    assert a.min() >= 0.7 - 1e-6                     # background + non-negative blobs
+    assert np.count_nonzero(a == 1.0) > 10 * 16 * 16  # ten macro blocks of >= side/32 squared
