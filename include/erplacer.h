@@ -202,6 +202,27 @@ erp_status erp_get_array(erp_ctx *ctx, erp_array which, void *dst, size_t bytes)
 /* Block until the context's stream is idle. */
 erp_status erp_synchronize(erp_ctx *ctx);
 
+/* ---- headless snapshots (src/drawing.rs:7-60 draw_placement,
+ * src/epotential.rs:199-223 draw_density_map), rasterised on the device into
+ * RGB bytes; the caller writes the image file (no graphics API).
+ * Placement: width = ceil(die_w), height = ceil(die_h) pixels, one pixel per
+ * unit; white background, movable instances blue, fixed red, later instances
+ * over earlier ones, zero-size instances skipped, row 0 at the top.
+ * Density: m x n pixels (bin (i, j) at column i, row n-1-j) of the density map
+ * of the current positions, min-max normalised, blue (low) to red (high). ---- */
+erp_status erp_snapshot_size(erp_ctx *ctx, int32_t *width, int32_t *height);
+erp_status erp_snapshot_placement(erp_ctx *ctx, uint8_t *rgb, size_t bytes);   /* width*height*3 */
+erp_status erp_snapshot_density(erp_ctx *ctx, uint8_t *rgb, size_t bytes);     /* m*n*3 */
+
+/* ---- checkpoint / resume (no counterpart in the reference): the state one
+ * Placement::step hands to the next -- positions, the Nesterov history and the
+ * scheduler / optimiser scalars -- in a versioned host buffer.  Restoring into
+ * a context of the same design and bin grid continues the run bit-identically;
+ * other buffers are rejected with ERP_EINVAL. ---- */
+erp_status erp_checkpoint_size(erp_ctx *ctx, size_t *bytes);
+erp_status erp_checkpoint(erp_ctx *ctx, void *buf, size_t bytes);
+erp_status erp_restore(erp_ctx *ctx, const void *buf, size_t bytes);
+
 /* ---- batched instances ----
  * Many designs advance together (the reference drives one design from its CLI
  * loop, src/main.rs:78-90; here that loop runs for a whole table of designs).

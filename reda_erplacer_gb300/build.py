@@ -25,6 +25,7 @@ CU_SOURCES = {
     "k_spectral.cu": [],
     "erp_api.cu": [],
     "erp_noalloc.cu": [],
+    "k_snapshot.cu": [],
 }
 CPP_SOURCES = ["synth.cpp"]
 HEADERS = ["erp_internal.cuh", "reduce.cuh", "bulk_copy.cuh"]

@@ -835,6 +835,137 @@ extern "C" erp_status erp_profile_stages(erp_ctx *ctx, int32_t reps, float *ms_o
 }
 
 // ---------------------------------------------------------------------------
+// headless snapshots (src/drawing.rs:7-60, src/epotential.rs:199-223)
+extern "C" erp_status erp_snapshot_size(erp_ctx *ctx, int32_t *width, int32_t *height) {
+    CTX_CHECK();
+    if (!width || !height) return ERP_EINVAL;
+    const double w = ceil((double)c.die_w), h = ceil((double)c.die_h);
+    if (!(w >= 1.0) || !(h >= 1.0) || w * h > (double)(1u << 30)) {
+        c.err = "die too large for a one-pixel-per-unit image";
+        return ERP_EINVAL;
+    }
+    *width = (int32_t)w;
+    *height = (int32_t)h;
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_snapshot_placement(erp_ctx *ctx, uint8_t *rgb, size_t bytes) {
+    int32_t W = 0, H = 0;
+    erp_status st = erp_snapshot_size(ctx, &W, &H);
+    if (st != ERP_OK) return st;
+    Ctx &c = ctx->c;
+    const size_t npix = (size_t)W * H;
+    if (!rgb || bytes < 3 * npix) { c.err = "destination smaller than width * height * 3"; return ERP_EINVAL; }
+    int *d_top = nullptr;
+    unsigned char *d_rgb = nullptr;
+    CK(cudaMallocAsync((void **)&d_top, sizeof(int) * npix, c.stream));
+    CK(cudaMallocAsync((void **)&d_rgb, 3 * npix, c.stream));
+    cudaError_t e = launch_snapshot_placement(c, W, H, d_rgb, d_top);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rgb, d_rgb, 3 * npix, cudaMemcpyDeviceToHost, c.stream);
+    cudaFreeAsync(d_top, c.stream);
+    cudaFreeAsync(d_rgb, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) { c.err = cudaGetErrorString(e); return ERP_ECUDA; }
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_snapshot_density(erp_ctx *ctx, uint8_t *rgb, size_t bytes) {
+    CTX_CHECK();
+    const size_t mn = (size_t)c.m * c.n;
+    if (!rgb || bytes < 3 * mn) { c.err = "destination smaller than m * n * 3"; return ERP_EINVAL; }
+    // the density map of the current positions (as erp_potential stores it)
+    enqueue_potential(c, true, false);
+    unsigned char *d_rgb = nullptr;
+    unsigned *d_mm = nullptr;
+    CK(cudaMallocAsync((void **)&d_rgb, 3 * mn, c.stream));
+    CK(cudaMallocAsync((void **)&d_mm, 2 * sizeof(unsigned), c.stream));
+    cudaError_t e = launch_snapshot_density(c, c.rho, d_rgb, d_mm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rgb, d_rgb, 3 * mn, cudaMemcpyDeviceToHost, c.stream);
+    cudaFreeAsync(d_rgb, c.stream);
+    cudaFreeAsync(d_mm, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) { c.err = cudaGetErrorString(e); return ERP_ECUDA; }
+    return ERP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// checkpoint / resume: the state that carries from one Placement::step to the
+// next -- positions, Nesterov history (src/nesterov.rs:6-13) and every scalar
+// of the scheduler and optimiser (DevState) -- in a versioned host buffer.
+namespace {
+struct CkptHeader {
+    char magic[8];        // "ERPCKPT\0"
+    uint32_t version;     // 1
+    uint32_t state_bytes; // sizeof(DevState)
+    int32_t N, NM, P, E, m, n;
+};
+constexpr int kCkptArrays = 6;   // x, y, prev_x, prev_y, prev_gx, prev_gy
+size_t ckpt_bytes(const Ctx &c) {
+    return sizeof(CkptHeader) + sizeof(DevState) + (size_t)kCkptArrays * sizeof(float) * (size_t)c.N;
+}
+}  // namespace
+
+extern "C" erp_status erp_checkpoint_size(erp_ctx *ctx, size_t *bytes) {
+    CTX_CHECK();
+    if (!bytes) return ERP_EINVAL;
+    *bytes = ckpt_bytes(c);
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_checkpoint(erp_ctx *ctx, void *buf, size_t bytes) {
+    CTX_CHECK();
+    if (!buf || bytes < ckpt_bytes(c)) { c.err = "buffer smaller than erp_checkpoint_size"; return ERP_EINVAL; }
+    CkptHeader hd;
+    memset(&hd, 0, sizeof hd);
+    memcpy(hd.magic, "ERPCKPT", 8);
+    hd.version = 1;
+    hd.state_bytes = (uint32_t)sizeof(DevState);
+    hd.N = c.N; hd.NM = c.NM; hd.P = c.P; hd.E = c.E; hd.m = c.m; hd.n = c.n;
+    char *o = (char *)buf;
+    memcpy(o, &hd, sizeof hd);
+    o += sizeof hd;
+    CK(cudaMemcpyAsync(o, c.st, sizeof(DevState), cudaMemcpyDeviceToHost, c.stream));
+    o += sizeof(DevState);
+    const float *arr[kCkptArrays] = {c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy};
+    for (const float *a : arr) {
+        CK(cudaMemcpyAsync(o, a, sizeof(float) * c.N, cudaMemcpyDeviceToHost, c.stream));
+        o += sizeof(float) * c.N;
+    }
+    CK(cudaStreamSynchronize(c.stream));
+    return ERP_OK;
+}
+
+extern "C" erp_status erp_restore(erp_ctx *ctx, const void *buf, size_t bytes) {
+    CTX_CHECK();
+    if (!buf || bytes < sizeof(CkptHeader)) { c.err = "not a checkpoint"; return ERP_EINVAL; }
+    CkptHeader hd;
+    memcpy(&hd, buf, sizeof hd);
+    if (memcmp(hd.magic, "ERPCKPT", 8) != 0 || hd.version != 1 || hd.state_bytes != sizeof(DevState)) {
+        c.err = "not a checkpoint of this library version";
+        return ERP_EINVAL;
+    }
+    if (hd.N != c.N || hd.NM != c.NM || hd.P != c.P || hd.E != c.E || hd.m != c.m || hd.n != c.n) {
+        c.err = "checkpoint of a different design or bin grid";
+        return ERP_EINVAL;
+    }
+    if (bytes < ckpt_bytes(c)) { c.err = "truncated checkpoint"; return ERP_EINVAL; }
+    const char *i = (const char *)buf + sizeof hd;
+    memcpy(c.h_st, i, sizeof(DevState));
+    CK(cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream));
+    i += sizeof(DevState);
+    float *arr[kCkptArrays] = {c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy};
+    for (float *a : arr) {
+        CK(cudaMemcpyAsync(a, i, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+        i += sizeof(float) * c.N;
+    }
+    launch_pack_xy(c);
+    c.map_dirty = true;   // the next step starts from a cleared map
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c.stream));
+    return ERP_OK;
+}
+
+// ---------------------------------------------------------------------------
 // batched instances: one graph, one branch per instance
 struct erp_batch {
     std::vector<erp_ctx *> ctx;

@@ -122,6 +122,9 @@ constexpr int kMaxPartials = 8192;
 // wirelength (src/hpwl.rs)
 void launch_wirelength(Ctx &c, float gamma_arg);          // gamma_arg < 0: read DevState.gamma
 void launch_pack_xy(Ctx &c);                               // xy from x, y after a host write
+// headless snapshots (k_snapshot.cu): RGB bytes on the device
+cudaError_t launch_snapshot_placement(Ctx &c, int W, int H, unsigned char *d_rgb, int *d_top);
+cudaError_t launch_snapshot_density(Ctx &c, const float *map, unsigned char *d_rgb, unsigned *d_mm);
 void launch_wl_gather(Ctx &c);
 // density + spectral + force (src/density.rs, src/epotential.rs, src/eforce.rs)
 void launch_initial_density(Ctx &c, const float *hx, const float *hy, const float *hw,

@@ -120,6 +120,12 @@ EXPORTS = {
     "erp_set_nesterov_history": (C.c_int, [C.c_void_p, f32p, f32p, f32p, f32p]),
     "erp_get_array": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
     "erp_synchronize": (C.c_int, [C.c_void_p]),
+    "erp_snapshot_size": (C.c_int, [C.c_void_p, i32p, i32p]),
+    "erp_snapshot_placement": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "erp_snapshot_density": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "erp_checkpoint_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
+    "erp_checkpoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "erp_restore": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "erp_profile_stages": (C.c_int, [C.c_void_p, C.c_int32, f32p]),
     "erp_spectral_create": (C.c_int, [C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_int32,
                                       C.c_void_p, C.POINTER(C.c_void_p)]),

@@ -18,6 +18,14 @@ import numpy as np
 from . import lib as L
 
 
+def write_ppm(path, img):
+    """Binary PPM (P6) of an (height, width, 3) uint8 image."""
+    h, w, _ = img.shape
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (w, h))
+        f.write(np.ascontiguousarray(img, np.uint8).tobytes())
+
+
 class Placement:
     def __init__(self, design, num_bins=(512, 512), target_density=-1.0,
                  start_mode=L.START_CENTER, device=0, stream=None):
@@ -136,6 +144,41 @@ class Placement:
         x = np.ascontiguousarray(x, np.float32)
         y = np.ascontiguousarray(y, np.float32)
         self._ck(self.lib.erp_set_positions(self.h, x.ctypes.data_as(L.f32p), y.ctypes.data_as(L.f32p)))
+
+    # -- checkpoint / resume --
+    def checkpoint(self):
+        """The state one step hands to the next, as bytes (erp_checkpoint)."""
+        n = C.c_size_t()
+        self._ck(self.lib.erp_checkpoint_size(self.h, C.byref(n)))
+        buf = (C.c_char * n.value)()
+        self._ck(self.lib.erp_checkpoint(self.h, buf, n.value))
+        return bytes(buf)
+
+    def restore(self, blob):
+        """Continue from a checkpoint of the same design and bin grid (erp_restore)."""
+        buf = (C.c_char * len(blob)).from_buffer_copy(blob)
+        self._ck(self.lib.erp_restore(self.h, buf, len(blob)))
+
+    # -- headless snapshots --
+    def snapshot_placement(self, path=None):
+        """draw_placement (src/drawing.rs:7-60) as an (height, width, 3) uint8
+        array rasterised on the device; written as a binary PPM when path is given."""
+        w, h = C.c_int32(), C.c_int32()
+        self._ck(self.lib.erp_snapshot_size(self.h, C.byref(w), C.byref(h)))
+        img = np.empty((h.value, w.value, 3), np.uint8)
+        self._ck(self.lib.erp_snapshot_placement(self.h, img.ctypes.data_as(C.c_void_p), img.nbytes))
+        if path:
+            write_ppm(path, img)
+        return img
+
+    def snapshot_density(self, path=None):
+        """draw_density_map (src/epotential.rs:199-223) of the current positions as an
+        (n, m, 3) uint8 array; written as a binary PPM when path is given."""
+        img = np.empty((self.n, self.m, 3), np.uint8)
+        self._ck(self.lib.erp_snapshot_density(self.h, img.ctypes.data_as(C.c_void_p), img.nbytes))
+        if path:
+            write_ppm(path, img)
+        return img
 
     def set_nesterov_history(self, px, py, pgx, pgy):
         a = [np.ascontiguousarray(t, np.float32) for t in (px, py, pgx, pgy)]
