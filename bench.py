@@ -251,50 +251,75 @@ def poisson_fp64(rho, bw, bh):
     return fx, fy, psi
 
 
+def measured_peak_tflops():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
 def spectral_section(args, device):
     """Isolated Poisson solve on the seeded density maps (0.7 background, 2,000
-    Gaussian blobs, 10 macro blocks) at 512^2, 1024^2 and 2048^2 bins: FP32 FFT
-    path, time per solve (CUDA events, L2 flushed before each solve), the
-    roofline on 16 B per bin (rho in; field_x, field_y, psi out) and the relative
-    L2 error of each output against the FP64 closed form."""
+    Gaussian blobs, 10 macro blocks) at 512^2, 1024^2 and 2048^2 bins, in the
+    three forms: FP32 FFT, TF32 DCT-GEMM and BF16 hi/lo DCT-GEMM (tcgen05).
+    Time per solve (CUDA events, L2 flushed before each solve), the relative L2
+    error of each output against the FP64 closed form, and the roofline: the
+    FFT on 16 B per bin (rho in; field_x, field_y, psi out) against HBM, the
+    contractions on 16 s^3 FLOP (x3 tensor products for BF16 hi/lo) against the
+    measured bf16 tensor peak (TF32: half of it, the nominal ratio)."""
     import numpy as np
     import torch
     import reda_erplacer_gb300 as R
     peak, peak_kind = measured_peak_gbs()
+    tpeak, tpeak_kind = measured_peak_tflops()
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device=f"cuda:{device}")
+    forms = (("fp32_fft", R.lib.PREC_FP32), ("tf32_dct_gemm", R.lib.PREC_TF32_GEMM),
+             ("bf16x3_dct_gemm", R.lib.PREC_BF16X3_GEMM))
     out = {}
     for side in (512, 1024, 2048):
         rho = R.workload_spectral(side, seed=3000 + side)
         ref = poisson_fp64(rho, 1.0, 1.0)
-        s = torch.cuda.Stream(device=device)
-        sol = R.SpectralSolver(side, side, 1.0, 1.0, stream=s.cuda_stream)
         r = torch.tensor(rho, device=f"cuda:{device}")
-        outs = [torch.empty_like(r) for _ in range(3)]
-        ptrs = [t.data_ptr() for t in outs]
-        with torch.cuda.stream(s):
-            for _ in range(3):
-                sol.solve(r.data_ptr(), *ptrs)
-            ts = []
-            for _ in range(args.spectral_reps):
-                flush.fill_(1.0)
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(s)
-                sol.solve(r.data_ptr(), *ptrs)
-                e1.record(s)
-                e1.synchronize()
-                ts.append(e0.elapsed_time(e1))
-        torch.cuda.synchronize()
-        got = [t.cpu().numpy().astype(np.float64) for t in outs]
-        err = [float(np.linalg.norm(g - w) / np.linalg.norm(w)) for g, w in zip(got, ref)]
-        us = 1000.0 * float(np.median(ts))
-        achieved = 16.0 * side * side / (us * 1e-6) / 1e9
-        out[f"{side}x{side}"] = {
-            "fp32_fft": {"us_per_solve": us, "achieved_gbs": achieved, "frac": achieved / peak,
-                         "peak_kind": peak_kind, "err_field_x": err[0], "err_field_y": err[1],
-                         "err_potential": err[2]},
-            "tf32_dct_gemm": "not built", "bf16x3_dct_gemm": "not built"}
-        sol.close()
+        row = {}
+        for name, prec in forms:
+            s = torch.cuda.Stream(device=device)
+            sol = R.SpectralSolver(side, side, 1.0, 1.0, stream=s.cuda_stream, precision=prec)
+            outs = [torch.empty_like(r) for _ in range(3)]
+            ptrs = [t.data_ptr() for t in outs]
+            with torch.cuda.stream(s):
+                for _ in range(3):
+                    sol.solve(r.data_ptr(), *ptrs)
+                ts = []
+                for _ in range(args.spectral_reps):
+                    flush.fill_(1.0)
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(s)
+                    sol.solve(r.data_ptr(), *ptrs)
+                    e1.record(s)
+                    e1.synchronize()
+                    ts.append(e0.elapsed_time(e1))
+            torch.cuda.synchronize()
+            got = [t.cpu().numpy().astype(np.float64) for t in outs]
+            err = [float(np.linalg.norm(g - w) / np.linalg.norm(w)) for g, w in zip(got, ref)]
+            us = 1000.0 * float(np.median(ts))
+            entry = {"us_per_solve": us, "err_field_x": err[0], "err_field_y": err[1], "err_potential": err[2]}
+            if prec == R.lib.PREC_FP32:
+                achieved = 16.0 * side * side / (us * 1e-6) / 1e9
+                entry.update({"bound": "hbm", "achieved_gbs": achieved, "frac": achieved / peak,
+                              "peak_kind": peak_kind})
+            else:
+                flops = 16.0 * float(side) ** 3 * (3 if prec == R.lib.PREC_BF16X3_GEMM else 1)
+                tfs = flops / (us * 1e-6) / 1e12
+                pk = tpeak if prec == R.lib.PREC_BF16X3_GEMM else tpeak / 2.0
+                entry.update({"bound": "tensor", "tensor_tflops": tfs, "peak_tflops": pk, "frac": tfs / pk,
+                              "peak_kind": tpeak_kind if prec == R.lib.PREC_BF16X3_GEMM
+                              else tpeak_kind + " bf16 / 2 (tf32 nominal ratio)"})
+            row[name] = entry
+            sol.close()
+        out[f"{side}x{side}"] = row
     return out
 
 

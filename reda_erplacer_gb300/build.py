@@ -26,6 +26,7 @@ CU_SOURCES = {
     "erp_api.cu": [],
     "erp_noalloc.cu": [],
     "k_snapshot.cu": [],
+    "k_dctgemm.cu": [],
 }
 CPP_SOURCES = ["synth.cpp"]
 HEADERS = ["erp_internal.cuh", "reduce.cuh", "bulk_copy.cuh"]

@@ -25,6 +25,7 @@ struct erp_spectral {
     SpectralPlan p;
     DevState *st;
     std::string err;
+    DctGemmPlan *gemm = nullptr;   // tensor-core precisions
 };
 
 static thread_local std::string g_create_err;
@@ -1548,14 +1549,29 @@ extern "C" erp_status erp_spectral_create(int32_t m, int32_t n, float bin_w, flo
         g_create_err = "invalid spectral solve parameters";
         return ERP_EINVAL;
     }
-    if (precision != ERP_PREC_FP32) {
+    if (precision != ERP_PREC_FP32 && precision != ERP_PREC_TF32_GEMM && precision != ERP_PREC_BF16X3_GEMM) {
         g_create_err = "unsupported precision";
         return ERP_ENOTSUP;
+    }
+    if (precision != ERP_PREC_FP32 && (m % 128 || n % 128)) {
+        g_create_err = "the tensor-core solve needs bin counts that are multiples of 128";
+        return ERP_EINVAL;
     }
     int dev = 0;
     cudaGetDevice(&dev);
     erp_status s = check_device(dev, g_create_err);
     if (s != ERP_OK) return s;
+    if (precision != ERP_PREC_FP32) {
+        erp_spectral *sg = new erp_spectral();
+        sg->gemm = dctgemm_create(m, n, bin_w, bin_h, precision == ERP_PREC_TF32_GEMM ? 0 : 1,
+                                  (cudaStream_t)stream, g_create_err);
+        if (!sg->gemm) {
+            delete sg;
+            return ERP_ECUDA;
+        }
+        *out = sg;
+        return ERP_OK;
+    }
     if (spectral_prepare() != cudaSuccess) { g_create_err = "cudaFuncSetAttribute failed"; return ERP_ECUDA; }
     erp_spectral *sp = new erp_spectral();
     SpectralPlan &p = sp->p;
@@ -1590,6 +1606,18 @@ extern "C" erp_status erp_spectral_create(int32_t m, int32_t n, float bin_w, flo
 extern "C" erp_status erp_spectral_solve(erp_spectral *sp, const float *rho, float *fx, float *fy,
                                          float *psi) {
     if (!sp || !rho || !fx || !fy) return ERP_EINVAL;
+    if (sp->gemm) {
+        const cudaError_t eg = dctgemm_solve(*sp->gemm, rho, fx, fy, psi);
+        if (eg == cudaErrorTimeout) {
+            sp->err = "a bounded wait of the tensor-core solve ran out";
+            return ERP_ETIMEDOUT;
+        }
+        if (eg != cudaSuccess) {
+            sp->err = cudaGetErrorString(eg);
+            return ERP_ECUDA;
+        }
+        return ERP_OK;
+    }
     SpectralArgs a;
     a.rho_in = rho;
     a.fx = fx;
@@ -1607,6 +1635,7 @@ extern "C" erp_status erp_spectral_solve(erp_spectral *sp, const float *rho, flo
 
 extern "C" void erp_spectral_destroy(erp_spectral *sp) {
     if (!sp) return;
+    if (sp->gemm) dctgemm_destroy(sp->gemm);
     SpectralPlan &p = sp->p;
     void *ptrs[] = {p.t1, p.tx, p.ty, p.tp, p.tw_m, p.tw_n, p.ek_m, p.ek_n, p.wu, p.wv, sp->st};
     for (void *q : ptrs)

@@ -168,6 +168,12 @@ struct SpectralArgs {
 };
 void launch_spectral_plan(const SpectralPlan &p, const SpectralArgs &a);
 cudaError_t spectral_prepare();
+// tensor-core form of the spectral solve (k_dctgemm.cu): kind 0 TF32, 1 BF16x3
+struct DctGemmPlan;
+DctGemmPlan *dctgemm_create(int m, int n, float bin_w, float bin_h, int kind, cudaStream_t stream,
+                            std::string &err);
+cudaError_t dctgemm_solve(DctGemmPlan &P, const float *rho, float *fx, float *fy, float *psi);
+void dctgemm_destroy(DctGemmPlan *P);
 cudaError_t place_prepare();   // opt the density scatter into its dynamic shared memory
 size_t spectral_smem_bytes(int m, int n);
 

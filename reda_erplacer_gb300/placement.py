@@ -249,12 +249,14 @@ class Batch:
 
 
 class SpectralSolver:
-    """Standalone Poisson solve (src/epotential.rs:284-343) on device pointers."""
+    """Standalone Poisson solve (src/epotential.rs:284-343) on device pointers.
+    precision: lib.PREC_FP32 (FFT), PREC_TF32_GEMM or PREC_BF16X3_GEMM (DCT
+    matrix contractions on the tensor cores; bin counts multiples of 128)."""
 
-    def __init__(self, m, n, bin_w, bin_h, stream=None):
+    def __init__(self, m, n, bin_w, bin_h, stream=None, precision=L.PREC_FP32):
         self.lib = L.load()
         h = C.c_void_p()
-        L.check(self.lib.erp_spectral_create(int(m), int(n), float(bin_w), float(bin_h), L.PREC_FP32,
+        L.check(self.lib.erp_spectral_create(int(m), int(n), float(bin_w), float(bin_h), int(precision),
                                              C.c_void_p(stream) if stream else None, C.byref(h)))
         self.h = h
 

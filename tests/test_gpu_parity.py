@@ -264,3 +264,35 @@ def test_batch_matches_individual_runs(R):
     its2, _ = bt.run(3, 0.0)
     assert its2 == [3] * len(mix)
     bt.close()
+
+
+@pytest.mark.parametrize("m,n", [(256, 256), (512, 1024), (1024, 512)])
+@pytest.mark.parametrize("prec,bound", [(1, 3e-2), (2, 5e-3)])
+def test_spectral_tensor_core_forms(R, O, m, n, prec, bound):
+    """DCT/IDXST contractions on the tensor cores (TF32; BF16 hi/lo x3) against
+    the FP64 solve on white-noise maps (the hardest case for a contraction: every
+    output sums K terms of order one that cancel); without psi too.  Measured on
+    these inputs: TF32 ~1e-2, BF16x3 ~2e-3; on the smooth isolated-solve maps
+    2e-3 and 3e-5..6e-4 (reported by the benchmark)."""
+    import torch
+    rng = np.random.default_rng(m + 5 * n + prec)
+    rho = (0.5 + rng.random((m, n))).astype(np.float32)
+    bw, bh = 1.1, 0.8
+    want = O.poisson(rho, bw, bh, dtype=np.float64)
+    sol = R.SpectralSolver(m, n, bw, bh, precision=prec)
+    r = torch.tensor(rho, device="cuda")
+    out = [torch.empty_like(r) for _ in range(3)]
+    sol.solve(r.data_ptr(), *[t.data_ptr() for t in out])
+    torch.cuda.synchronize()
+    for got, w in zip(out, want):
+        assert rel_l2(got.cpu().numpy(), w) <= bound
+    out2 = [torch.empty_like(r) for _ in range(2)]
+    sol.solve(r.data_ptr(), out2[0].data_ptr(), out2[1].data_ptr(), None)
+    torch.cuda.synchronize()
+    assert torch.equal(out2[0], out[0]) and torch.equal(out2[1], out[1])
+    sol.close()
+
+
+def test_spectral_tensor_core_rejects_odd_sizes(R):
+    with pytest.raises(R.ErpError):
+        R.SpectralSolver(64, 256, 1.0, 1.0, precision=1)
