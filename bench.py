@@ -323,6 +323,50 @@ def spectral_section(args, device):
     return out
 
 
+def mixed_section(args, device, d, cfg, sc_fp32, tto_fp32):
+    """The 1M-cell design end to end with the spectral solve on the tensor cores
+    (TF32; BF16 hi/lo x3), against the plain FP32 path: iterations/s over the
+    same number of iterations as the timed FP32 run (plus its warm-up); HPWL and
+    overflow at the FP32 path's time-to-overflow-0.10 iteration count (the end
+    of the run lies in the reference loop's diverging phase, where any
+    perturbation grows); and the time to overflow 0.10 from a fresh context."""
+    import torch
+    import reda_erplacer_gb300 as R
+    m, n = cfg["bins"]
+    iters = int(sc_fp32["iteration"])
+    ref_it = tto_fp32["iterations"] if tto_fp32 else None
+    out = {"iterations": iters, "compare_at_iteration": ref_it,
+           "fp32": {"hpwl": tto_fp32["hpwl"] if tto_fp32 else None,
+                    "overflow": tto_fp32["overflow"] if tto_fp32 else None}}
+    for name, prec in (("tf32_dct_gemm", R.lib.PREC_TF32_GEMM), ("bf16x3_dct_gemm", R.lib.PREC_BF16X3_GEMM)):
+        entry = {}
+        pl = R.Placement(d, (m, n), cfg["target_density"], start_mode=1, device=device, precision=prec)
+        pl.synchronize()
+        t0 = time.perf_counter()
+        it, _ = pl.run(iters, stop_overflow=0.0)
+        pl.synchronize()
+        entry["iters_per_s"] = it / (time.perf_counter() - t0)
+        pl.close()
+        if ref_it:
+            pc = R.Placement(d, (m, n), cfg["target_density"], start_mode=1, device=device, precision=prec)
+            _, lc = pc.run(ref_it, stop_overflow=0.0)
+            pc.close()
+            entry.update({"hpwl": lc["hpwl"], "overflow": lc["overflow"],
+                          "hpwl_rel_diff": (lc["hpwl"] - tto_fp32["hpwl"]) / tto_fp32["hpwl"],
+                          "overflow_abs_diff": lc["overflow"] - tto_fp32["overflow"]})
+        pt = R.Placement(d, (m, n), cfg["target_density"], start_mode=1, device=device, precision=prec)
+        pt.synchronize()
+        t0 = time.perf_counter()
+        it_t, last_t = pt.run(cfg["iterations"], stop_overflow=0.10)
+        pt.synchronize()
+        entry["time_to_overflow"] = {"reached": bool(last_t["overflow"] <= 0.10), "iterations": it_t,
+                                     "seconds": time.perf_counter() - t0}
+        pt.close()
+        out[name] = entry
+    torch.cuda.synchronize()
+    return out
+
+
 class LazyJobs:
     """The serving stream's jobs, generated on a thread pool just ahead of use
     (at most `ahead` outstanding); the server copies a design when it is
@@ -531,6 +575,8 @@ def run_ours(args):
         line["batched"] = batch_section(args, local)
     if not args.no_spectral:
         line["spectral_solve"] = spectral_section(args, local)
+    if not args.no_mixed:
+        line["mixed_form"] = mixed_section(args, local, d, cfg, sc, tto)
     if args.serve_jobs > 0:
         line["serving"] = serve_section(args, local)
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -559,6 +605,7 @@ def main():
     ap.add_argument("--batch-iters", type=int, default=600)
     ap.add_argument("--no-tto", action="store_true", help="skip the time-to-overflow-0.10 run")
     ap.add_argument("--no-spectral", action="store_true", help="skip the isolated-solve section")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision end-to-end runs")
     ap.add_argument("--spectral-reps", type=int, default=20)
     ap.add_argument("--serve-jobs", type=int, default=2000, help="jobs of the serving stream (0: skip)")
     args = ap.parse_args()

@@ -76,8 +76,8 @@ typedef enum erp_start_mode {
 typedef enum erp_precision {
     ERP_PREC_FP32 = 0,        /* FP32 spectral solve (FFT-based DCT/DST), the parity path */
     ERP_PREC_TF32_GEMM = 1,   /* spectral solve as DCT/IDXST matrix contractions on tcgen05, TF32
-                                 operands, FP32 accumulation (erp_spectral_create only; bins
-                                 multiples of 128); relative error ~1e-3 against FP64 */
+                                 operands, FP32 accumulation (erp_spectral_create and placement
+                                 contexts; bins multiples of 128); ~2e-3 against FP64 */
     ERP_PREC_BF16X3_GEMM = 2  /* same contractions with bf16 hi/lo split operands, three products
                                  hi.hi + hi.lo + lo.hi, FP32 accumulation; ~1e-5 against FP64 */
 } erp_precision;

@@ -158,6 +158,7 @@ void free_ctx(Ctx &c) {
         else cudaFree(p);
     }
     if (c.h_st) cudaFreeHost(c.h_st);
+    if (c.gemm) dctgemm_destroy(c.gemm);   // synchronises the stream before freeing
     if (c.graph_ready) cudaGraphExecDestroy(c.graph);
     if (c.own_stream && c.stream) cudaStreamDestroy(c.stream);
     delete[] c.h_slot_of_pin;
@@ -193,6 +194,11 @@ void launch_spectral(Ctx &c, bool zero_map, bool store_rho, bool want_psi) {
     a.psi = want_psi ? c.psi : nullptr;
     a.partials = c.partials;
     a.st = c.st;
+    if (c.gemm) {   // tensor-core precisions: rho, then the contractions (rho_out is c.rho itself)
+        launch_map_rho(a, (size_t)c.m * c.n, c.rho, c.stream);
+        dctgemm_solve(*c.gemm, c.rho, c.fx, c.fy, a.psi, &c.st->status);
+        return;
+    }
     launch_spectral_plan(plan_of(c), a);
 }
 }  // namespace erp
@@ -216,9 +222,14 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
         c.err = "bin counts must be powers of two in [16, 4096]";
         return ERP_EINVAL;
     }
-    if (prm.precision != ERP_PREC_FP32) {
+    if (prm.precision != ERP_PREC_FP32 && prm.precision != ERP_PREC_TF32_GEMM &&
+        prm.precision != ERP_PREC_BF16X3_GEMM) {
         c.err = "unsupported precision";
         return ERP_ENOTSUP;
+    }
+    if (prm.precision != ERP_PREC_FP32 && (prm.num_bins_x % 128 || prm.num_bins_y % 128)) {
+        c.err = "the tensor-core spectral solve needs bin counts that are multiples of 128";
+        return ERP_EINVAL;
     }
     erp_status s = validate(d, c.err);
     if (s != ERP_OK) return s;
@@ -368,6 +379,11 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     CK(cudaMallocHost((void **)&c.h_st, sizeof(DevState)));
     spectral_tables(c.m, c.n, c.bin_w, c.bin_h, &c.tw_m, &c.tw_n, &c.ek_m, &c.ek_n, &c.wu, &c.wv, c.stream);
     CK(cudaGetLastError());
+    if (prm.precision != ERP_PREC_FP32) {
+        c.gemm = dctgemm_create(c.m, c.n, c.bin_w, c.bin_h, prm.precision == ERP_PREC_TF32_GEMM ? 0 : 1, c.stream,
+                                c.err);
+        if (!c.gemm) return ERP_ECUDA;
+    }
     // --- uploads ---
     CK(upload(c.x, hx.data(), sizeof(float) * N, c.stream));
     CK(upload(c.y, hy.data(), sizeof(float) * N, c.stream));
@@ -1228,6 +1244,10 @@ extern "C" erp_status erp_estimate_footprint(const erp_design *d, const erp_para
     b += al(4 * P) + 2 * al(8 * P) + al(4 * (E + 1)) + al(4 * E) + al(4 * (NM + 1)) + al(4 * movable_pins);
     b += al(8 * mn) + 9 * al(4 * mn) + al(8 * (int64_t)kMaxPartials) + al(sizeof(DevState));
     b += al(8 * (m / 2)) + al(8 * (n / 2)) + al(8 * m) + al(8 * n) + al(4 * m) + al(4 * n);
+    if (pp && pp->precision != ERP_PREC_FP32) {   // tensor-core plan: 4 transforms per axis + 7 map buffers
+        const int64_t es = pp->precision == ERP_PREC_TF32_GEMM ? 4 : 4;   // fp32, or bf16 hi + lo
+        b += es * (2 * (int64_t)m * m + 2 * (int64_t)n * n + (int64_t)m * m + (int64_t)n * n) + es * 7 * mn;
+    }
     *bytes = b;
     return ERP_OK;
 }
@@ -1607,7 +1627,7 @@ extern "C" erp_status erp_spectral_solve(erp_spectral *sp, const float *rho, flo
                                          float *psi) {
     if (!sp || !rho || !fx || !fy) return ERP_EINVAL;
     if (sp->gemm) {
-        const cudaError_t eg = dctgemm_solve(*sp->gemm, rho, fx, fy, psi);
+        const cudaError_t eg = dctgemm_solve(*sp->gemm, rho, fx, fy, psi, nullptr);
         if (eg == cudaErrorTimeout) {
             sp->err = "a bounded wait of the tensor-core solve ran out";
             return ERP_ETIMEDOUT;

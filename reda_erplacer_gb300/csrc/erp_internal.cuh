@@ -68,6 +68,8 @@ struct NetClass {
     int32_t slot0;         // first pin slot of the class
 };
 
+struct DctGemmPlan;   // tensor-core spectral solve (k_dctgemm.cu)
+
 struct Ctx {
     // --- sizes ---
     int32_t N, NM, P, E, NS;   // nodes, movable, pins, nets, pin slots (= P)
@@ -109,6 +111,7 @@ struct Ctx {
     int32_t max_partials;
     DevState *st;
     DevState *h_st;            // pinned host mirror
+    DctGemmPlan *gemm;         // tensor-core spectral solve (precision TF32 / BF16x3), else nullptr
     // --- graph ---
     cudaGraphExec_t graph;
     bool graph_ready;
@@ -167,12 +170,13 @@ struct SpectralArgs {
     DevState *st = nullptr;
 };
 void launch_spectral_plan(const SpectralPlan &p, const SpectralArgs &a);
+// the map -> rho conversion, overflow and zeroing of R1 alone (tensor-core precisions)
+void launch_map_rho(const SpectralArgs &a, size_t mn, float *rho, cudaStream_t s);
 cudaError_t spectral_prepare();
 // tensor-core form of the spectral solve (k_dctgemm.cu): kind 0 TF32, 1 BF16x3
-struct DctGemmPlan;
 DctGemmPlan *dctgemm_create(int m, int n, float bin_w, float bin_h, int kind, cudaStream_t stream,
                             std::string &err);
-cudaError_t dctgemm_solve(DctGemmPlan &P, const float *rho, float *fx, float *fy, float *psi);
+cudaError_t dctgemm_solve(DctGemmPlan &P, const float *rho, float *fx, float *fy, float *psi, int *status);
 void dctgemm_destroy(DctGemmPlan *P);
 cudaError_t place_prepare();   // opt the density scatter into its dynamic shared memory
 size_t spectral_smem_bytes(int m, int n);

@@ -490,8 +490,12 @@ static cudaError_t run_gemm(const DctGemmPlan &P, const GemmMaps &maps, const Ge
 // fx, fy (, psi) = Poisson solve of rho: four contraction launches (+ the split
 // of rho).  Returns cudaErrorTimeout when a bounded wait of an earlier solve
 // on this plan ran out (seen through the pinned mirror of the status word).
-cudaError_t dctgemm_solve(DctGemmPlan &P, const float *rho, float *fx, float *fy, float *psi) {
-    if (*(volatile int *)P.h_status) return cudaErrorTimeout;
+//
+// status: where the contractions report a bounded wait that ran out; nullptr
+// uses the plan's own word and its pinned mirror (a placement context passes
+// its DevState status, read by the host with the rest of the state).
+cudaError_t dctgemm_solve(DctGemmPlan &P, const float *rho, float *fx, float *fy, float *psi, int *status) {
+    if (!status && *(volatile int *)P.h_status) return cudaErrorTimeout;
     const int m = P.m, n = P.n, nk = psi ? 3 : 2;
     const size_t mn = (size_t)m * n;
     const bool split = P.kind == 1;
@@ -507,7 +511,7 @@ cudaError_t dctgemm_solve(DctGemmPlan &P, const float *rho, float *fx, float *fy
     }
     GemmEpi ep;
     memset(&ep, 0, sizeof ep);
-    ep.status = P.status;
+    ep.status = status ? status : P.status;
     ep.split = split ? 1 : 0;
     // G1: Z = rho C_n^T, stored transposed [n][m]
     ep.mode = 0; ep.transpose = 1; ep.alpha = 1.0f; ep.ldc = m;
@@ -527,6 +531,7 @@ cudaError_t dctgemm_solve(DctGemmPlan &P, const float *rho, float *fx, float *fy
     float *outs[3] = {fx, fy, psi};
     for (int k = 0; k < 3; ++k) { ep.out[k][0] = outs[k]; ep.out[k][1] = nullptr; }
     if ((e = run_gemm(P, P.g4, ep, m, n, m, nk, 128)) != cudaSuccess) return e;
+    if (status) return cudaSuccess;
     return cudaMemcpyAsync(P.h_status, P.status, sizeof(int), cudaMemcpyDeviceToHost, P.stream);
 }
 

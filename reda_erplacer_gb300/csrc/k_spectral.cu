@@ -998,6 +998,45 @@ __global__ void __launch_bounds__(G * kQ * 32) k_rows_inv_g(
                       gbar, [&](int i, float v) { out[i] = v; });
 }
 
+// The density map as rho for the tensor-core solve: the conversion of R1 (same
+// float rules, so rho is bit-identical to what the FFT path transforms), the
+// FP64 overflow sum with the last-block finalize, and the map zeroing.
+__global__ void __launch_bounds__(kThreads) k_map_rho(size_t mn, unsigned long long *__restrict__ dmap,
+                                                      const float *__restrict__ initial, float fixed_inv, float coef,
+                                                      float inv_area, int zero_map, float *__restrict__ rho,
+                                                      double *__restrict__ partials, DevState *__restrict__ st,
+                                                      double movable_area) {
+    __shared__ double shr[kThreads / 32];
+    if (st->done) return;
+    double ovf = 0.0;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < mn; idx += (size_t)gridDim.x * blockDim.x) {
+        const unsigned long long q = dmap[idx];
+        if (zero_map) dmap[idx] = 0ull;
+        // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
+        const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q), fixed_inv), initial[idx]);
+        const float o = __fsub_rn(d, coef);
+        ovf += (double)(o > 0.0f ? o : 0.0f);    // src/epotential.rs:274-276
+        rho[idx] = __fmul_rn(d, inv_area);         // src/epotential.rs:284-285
+    }
+    const double b = block_sum(ovf, shr);
+    double vals[1] = {b};
+    if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_OVF], gridDim.x)) {
+        const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
+        if (threadIdx.x == 0) {
+            st->overflow = tot;
+            st->overflow_f = (float)(tot / movable_area);
+            st->ctr[CTR_OVF] = 0;
+        }
+    }
+}
+
+void launch_map_rho(const SpectralArgs &a, size_t mn, float *rho, cudaStream_t s) {
+    size_t g = (mn + kThreads - 1) / kThreads;
+    if (g > 152 * 8) g = 152 * 8;
+    k_map_rho<<<(int)g, kThreads, 0, s>>>(mn, a.dmap, a.initial, a.fixed_inv, a.coef, a.inv_bin_area,
+                                          a.zero_map ? 1 : 0, rho, a.partials, a.st, a.movable_area);
+}
+
 int ilog2(int v) {
     int l = 0;
     while ((1 << l) < v) ++l;
