@@ -334,3 +334,25 @@ def test_step_mixed_precision_rejects_small_grids(R):
     d = small_synth(3000, seed=2)
     with pytest.raises(R.ErpError):
         R.Placement(d, (64, 64), 1.0, start_mode=1, precision=2)
+
+
+def test_mixed_precision_batch_matches_individual_runs(R):
+    """The mixed batched form (BF16x3 tensor-core solve where the grid allows,
+    FP32 FFT on 64^2) ends bit-identical to each design run alone in its form."""
+    mix = R.workload_batch(count=4, seed=78, min_cells=8000, max_cells=60000)
+    designs = [d for d, _ in mix]
+    bins = [b for _, b in mix]
+    precs = [2 if b[0] >= 128 else 0 for b in bins]
+    assert any(p == 2 for p in precs)
+    bt = R.Batch(designs, bins, 1.0, start_mode=1, precision=precs)
+    its, lasts = bt.run(120, stop_overflow=0.5)
+    for i, (d, b) in enumerate(mix):
+        g = R.Placement(d, b, 1.0, start_mode=1, precision=precs[i])
+        it, last = g.run(120, stop_overflow=0.5)
+        assert it == its[i]
+        assert last["hpwl"] == lasts[i]["hpwl"] and last["overflow"] == lasts[i]["overflow"]
+        xa, ya = g.positions()
+        xb, yb = bt.positions(i)
+        assert np.array_equal(xa, xb) and np.array_equal(ya, yb)
+        g.close()
+    bt.close()
