@@ -124,12 +124,14 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 }
 
 // Stage ring: A tile 128 x 128 bytes, B tile BN x 128 bytes (+ the lo parts
-// for BF16x3).  TF32 with BN = 64 fits two CTAs per SM.
+// for BF16x3).
 template <int KIND, int BN>
 struct GemmCfg {
     static constexpr int kABytes = kTile * 128, kBBytes = BN * 128;
     static constexpr int kStageBytes = (KIND == 0 ? 1 : 2) * (kABytes + kBBytes);
-    static constexpr int kStages = KIND == 0 ? 4 : 3;
+    // as many stages as fit (about 190 KB in flight per SM; TF32 128 x 64 tiles
+    // run two CTAs per SM)
+    static constexpr int kStages = KIND == 0 ? (BN == 128 ? 6 : 4) : (BN == 128 ? 3 : 4);
     static constexpr int kBK = KIND == 0 ? 32 : 64;             // K elements per stage (128 bytes)
     static constexpr size_t kSmem = (size_t)kStages * kStageBytes + 1024;
 };
@@ -214,49 +216,58 @@ __global__ void __launch_bounds__(128, 1) k_gemm_nt(const __grid_constant__ Gemm
     if (!ok && lane == 0) failed = 1;
     tc_fence_after();
     if (ok) {
+        // The stage ring is idle now (every MMA has completed): each warp
+        // transposes its 32 x 32 chunks through a 32 x 33 buffer there, so that
+        // row-major stores go out with consecutive columns across the lanes.
+        float *buf = reinterpret_cast<float *>(base) + warp * (32 * 33);
         const int r = warp * 32 + lane;   // this thread's accumulator row (TMEM lane)
         const int gr = tile_m + r;
+        const float al = epi.alpha;
         for (int c0 = 0; c0 < BN; c0 += 32) {
             float v[32];
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-            if (epi.mode == 0) {
-                const float al = epi.alpha;
+            if (epi.mode == 0 && epi.transpose) {   // C^T: lanes hold consecutive rows already
                 if (!epi.split) {
                     float *o = static_cast<float *>(epi.out[z][0]);
-                    if (!epi.transpose) {   // the thread's 32 columns are contiguous: 128-bit stores
-                        float4 *d = reinterpret_cast<float4 *>(o + (size_t)gr * epi.ldc + tile_n + c0);
 #pragma unroll
-                        for (int q = 0; q < 8; ++q)
-                            d[q] = make_float4(al * v[4 * q], al * v[4 * q + 1], al * v[4 * q + 2], al * v[4 * q + 3]);
-                    } else {                // lanes hold consecutive rows: coalesced per column
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) o[(size_t)(tile_n + c0 + j) * epi.ldc + gr] = al * v[j];
-                    }
+                    for (int j = 0; j < 32; ++j) o[(size_t)(tile_n + c0 + j) * epi.ldc + gr] = al * v[j];
                 } else {
                     __nv_bfloat16 *oh = static_cast<__nv_bfloat16 *>(epi.out[z][0]);
                     __nv_bfloat16 *ol = static_cast<__nv_bfloat16 *>(epi.out[z][1]);
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
-                        const int gc = tile_n + c0 + j;
-                        const size_t idx = epi.transpose ? (size_t)gc * epi.ldc + gr : (size_t)gr * epi.ldc + gc;
+                        const size_t idx = (size_t)(tile_n + c0 + j) * epi.ldc + gr;
                         const float x = al * v[j];
                         const __nv_bfloat16 h = __float2bfloat16_rn(x);
                         oh[idx] = h;
                         ol[idx] = __float2bfloat16_rn(x - __bfloat162float(h));
                     }
                 }
-            } else {   // weighted spectra: row u = gr, column v = gc (planes x, y, p)
-                const float wu = epi.wu[gr];
-                const bool three = epi.nplanes > 2;
+                continue;
+            }
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int gc = tile_n + c0 + j;
-                    const float wv = epi.wv[gc];
+            for (int j = 0; j < 32; ++j) buf[lane * 33 + j] = v[j];
+            __syncwarp();
+            const int gc = tile_n + c0 + lane;
+            const float wv = epi.mode == 1 ? epi.wv[gc] : 0.0f;
+            const bool three = epi.nplanes > 2;
+            for (int rr = 0; rr < 32; ++rr) {
+                const int gr2 = tile_m + warp * 32 + rr;
+                const size_t idx = (size_t)gr2 * epi.ldc + gc;
+                const float x = al * buf[rr * 33 + lane];
+                if (epi.mode == 0) {
+                    if (!epi.split) {
+                        static_cast<float *>(epi.out[z][0])[idx] = x;
+                    } else {
+                        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+                        static_cast<__nv_bfloat16 *>(epi.out[z][0])[idx] = h;
+                        static_cast<__nv_bfloat16 *>(epi.out[z][1])[idx] = __float2bfloat16_rn(x - __bfloat162float(h));
+                    }
+                } else {   // weighted spectra: row u = gr2, column v = gc (planes x, y, p)
+                    const float wu = epi.wu[gr2];
                     const float k2 = __fadd_rn(__fmul_rn(wu, wu), __fmul_rn(wv, wv));
-                    const float ik = (gr == 0 && gc == 0) ? 0.0f : __frcp_rn(k2);
-                    const float a = epi.alpha * v[j];
-                    const float px = a * (0.5f * wu * ik), py = a * (0.5f * wv * ik), pp = a * ik;
-                    const size_t idx = (size_t)gr * epi.ldc + gc;
+                    const float ik = (gr2 == 0 && gc == 0) ? 0.0f : __frcp_rn(k2);
+                    const float px = x * (0.5f * wu * ik), py = x * (0.5f * wv * ik), pp = x * ik;
                     if (!epi.split) {
                         static_cast<float *>(epi.out[0][0])[idx] = px;
                         static_cast<float *>(epi.out[1][0])[idx] = py;
@@ -276,6 +287,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm_nt(const __grid_constant__ Gemm
                     }
                 }
             }
+            __syncwarp();
         }
     }
     tc_fence_before();
