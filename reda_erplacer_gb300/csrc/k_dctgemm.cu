@@ -216,9 +216,11 @@ __global__ void __launch_bounds__(128, 1) k_gemm_nt(const __grid_constant__ Gemm
     if (!ok && lane == 0) failed = 1;
     tc_fence_after();
     if (ok) {
-        // The stage ring is idle now (every MMA has completed): each warp
-        // transposes its 32 x 32 chunks through a 32 x 33 buffer there, so that
-        // row-major stores go out with consecutive columns across the lanes.
+        // The stage ring is idle now (every MMA has completed): for the weighted
+        // spectra and split outputs each warp transposes its 32 x 32 chunks
+        // through a 32 x 33 buffer there, so that the many narrow row-major
+        // stores go out with consecutive columns across the lanes; plain fp32
+        // rows use 128-bit stores of the thread's own row.
         float *buf = reinterpret_cast<float *>(base) + warp * (32 * 33);
         const int r = warp * 32 + lane;   // this thread's accumulator row (TMEM lane)
         const int gr = tile_m + r;
@@ -243,6 +245,14 @@ __global__ void __launch_bounds__(128, 1) k_gemm_nt(const __grid_constant__ Gemm
                         ol[idx] = __float2bfloat16_rn(x - __bfloat162float(h));
                     }
                 }
+                continue;
+            }
+            if (epi.mode == 0 && !epi.split) {   // plain fp32 rows: the thread's 32 columns, 128-bit stores
+                float4 *d = reinterpret_cast<float4 *>(static_cast<float *>(epi.out[z][0]) + (size_t)gr * epi.ldc +
+                                                       tile_n + c0);
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    d[q] = make_float4(al * v[4 * q], al * v[4 * q + 1], al * v[4 * q + 2], al * v[4 * q + 3]);
                 continue;
             }
 #pragma unroll
