@@ -360,6 +360,66 @@ erp_status erp_synth_create(const erp_synth_params *p, erp_synth **out);
 erp_status erp_synth_design(const erp_synth *s, erp_design *d);
 void erp_synth_destroy(erp_synth *s);
 
+/* ---- LEF/DEF: ingest (replaces reda_db::read_db::<f32>(lef, def, verbose),
+ * src/main.rs:69), export, and the placed-DEF hand-off to legalisation (the
+ * step after global placement, which the reference does not write,
+ * README.md:23).  Host code only: these calls need no GPU.
+ *
+ * The design a netlist exposes (erp_netlist_design) follows the erp_design
+ * rules above: movable components (DEF status PLACED / UNPLACED) first in DEF
+ * order, then FIXED / COVER components, then the DEF PINS as zero-size fixed
+ * instances; microns with the DIEAREA's lower-left corner at the origin; a
+ * pin's offset is the centre of its LEF port shapes after ORIGIN and the
+ * component orientation; nets with at least one connection, the two-pin nets
+ * first; LEF geometry snapped to the LEF database grid.  Errors are ERP_EINVAL
+ * (ERP_ENOMEM) with "file:line: message" in erp_lefdef_last_error(). ---- */
+typedef struct erp_netlist erp_netlist;
+typedef struct erp_lefdef_stats {
+    int32_t num_nodes, num_movable, num_fixed, num_io;
+    int32_t num_nets, num_pins, num_macros;
+    int32_t num_dropped_nets;    /* NETS entries without a connection */
+    int32_t num_skipped_conns;   /* "( * pin )" wildcards and MUSTJOIN entries */
+    int32_t num_unplaced_io;     /* DEF PINS without a location (placed at the die corner) */
+    int32_t def_dbu, lef_dbu;    /* DEF UNITS DISTANCE MICRONS; the LEF snap grid */
+    int64_t die[4];              /* DIEAREA bounding box, DEF units: x0 y0 x1 y1 */
+} erp_lefdef_stats;
+
+/* Read LEF files in order (technology, then cells; a later MACRO of the same
+ * name replaces an earlier one), then the DEF.  The netlist keeps the DEF text
+ * for erp_def_write_placed. */
+erp_status erp_lefdef_read(const char *const *lef_paths, int32_t num_lef, const char *def_path, erp_netlist **out);
+/* The message of the last failed LEF/DEF call on this thread. */
+const char *erp_lefdef_last_error(void);
+/* Fills *d with pointers into the netlist's arrays (valid until destroy). */
+erp_status erp_netlist_design(const erp_netlist *nl, erp_design *d);
+erp_status erp_netlist_stats(const erp_netlist *nl, erp_lefdef_stats *s);
+/* Names in design order (NULL when out of range). */
+const char *erp_netlist_node_name(const erp_netlist *nl, int32_t instance);
+const char *erp_netlist_net_name(const erp_netlist *nl, int32_t net);
+
+/* A netlist of an in-memory design (e.g. erp_synth_design), for export:
+ * movable instances become PLACED components c<i>, sized fixed instances FIXED
+ * components m<i> of CLASS BLOCK macros, zero-size fixed instances with at most
+ * one pin DEF PINS p<k>; nets n<e>; one macro per distinct (size, pin offsets),
+ * pins P<j> in inst_pins order.  Coordinates snap to 1/dbu micron, so the
+ * netlist's own design (erp_netlist_design) is the design as LEF/DEF carries it,
+ * and reading the written files back gives that design exactly. */
+typedef struct erp_lefdef_params {
+    int32_t dbu;              /* database units per micron (0: 2000) */
+    float site_w, row_h;      /* core site for the SITE and ROW statements (0: none) */
+} erp_lefdef_params;
+erp_status erp_netlist_from_design(const erp_design *d, const erp_lefdef_params *p, erp_netlist **out);
+/* Write the netlist as LEF and/or DEF (either path may be NULL). */
+erp_status erp_lefdef_write(const erp_netlist *nl, const char *lef_path, const char *def_path);
+/* The placed DEF: movable instance k (design order, k < num_movable) at
+ * (x[k], y[k]) microns, written as "PLACED ( X Y ) orient" in DEF units (rounded
+ * to nearest).  For a netlist read from a DEF, the source text is copied
+ * byte for byte except those clauses (ROW, TRACKS, SPECIALNETS, routing ...
+ * are kept for the legaliser); for one made from a design, the DEF is written
+ * anew. */
+erp_status erp_def_write_placed(const erp_netlist *nl, const float *x, const float *y, const char *def_path);
+void erp_netlist_destroy(erp_netlist *nl);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,9 +7,10 @@ from .lib import ErpError
 from .design import (Design, bins_for_cells, synth, workload_batch, workload_large, workload_small,
                      workload_spectral)
 from .placement import Batch, Placement, SpectralSolver
+from .lefdef import Netlist, read_db, write_lefdef
 
 lib.load()
 
 __all__ = ["Design", "synth", "workload_small", "workload_large", "workload_batch", "workload_spectral",
            "bins_for_cells",
-           "Placement", "Batch", "SpectralSolver", "ErpError"]
+           "Placement", "Batch", "SpectralSolver", "ErpError", "Netlist", "read_db", "write_lefdef"]

@@ -17,6 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liberplacer_gb300.so")
+CLI = os.path.join(HERE, "erplacer_gb300")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 
@@ -28,21 +29,22 @@ CU_SOURCES = {
     "k_snapshot.cu": [],
     "k_dctgemm.cu": [],
 }
-CPP_SOURCES = ["synth.cpp"]
+CPP_SOURCES = ["synth.cpp", "lefdef.cpp"]
+CLI_SOURCE = "erplacer_cli.cpp"   # the command-line driver, linked against the library
 HEADERS = ["erp_internal.cuh", "reduce.cuh", "bulk_copy.cuh"]
 
 
 def _deps():
-    files = [os.path.join(CSRC, f) for f in list(CU_SOURCES) + CPP_SOURCES + HEADERS]
+    files = [os.path.join(CSRC, f) for f in list(CU_SOURCES) + CPP_SOURCES + [CLI_SOURCE] + HEADERS]
     files.append(os.path.join(INCLUDE, "erplacer.h"))
     files.append(os.path.abspath(__file__))
     return files
 
 
 def _stale():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return True
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI))
     return any(os.path.getmtime(f) > t for f in _deps())
 
 
@@ -79,6 +81,9 @@ def build(force=False, verbose=False):
             sys.stdout.write(o)
     _run([NVCC] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs)
     os.replace(LIB + ".tmp", LIB)
+    _run(["g++", "-O2", "-std=c++17", "-I", INCLUDE, os.path.join(CSRC, CLI_SOURCE), "-o", CLI + ".tmp",
+          "-L", HERE, "-l:" + os.path.basename(LIB), "-Wl,-rpath,$ORIGIN"])
+    os.replace(CLI + ".tmp", CLI)
     return LIB
 
 

@@ -90,6 +90,23 @@ class JobResult(C.Structure):
         return d
 
 
+class LefDefStats(C.Structure):
+    _fields_ = [("num_nodes", C.c_int32), ("num_movable", C.c_int32), ("num_fixed", C.c_int32),
+                ("num_io", C.c_int32), ("num_nets", C.c_int32), ("num_pins", C.c_int32),
+                ("num_macros", C.c_int32), ("num_dropped_nets", C.c_int32),
+                ("num_skipped_conns", C.c_int32), ("num_unplaced_io", C.c_int32),
+                ("def_dbu", C.c_int32), ("lef_dbu", C.c_int32), ("die", C.c_int64 * 4)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "die"}
+        d["die"] = tuple(int(v) for v in self.die)
+        return d
+
+
+class LefDefParams(C.Structure):
+    _fields_ = [("dbu", C.c_int32), ("site_w", C.c_float), ("row_h", C.c_float)]
+
+
 EXPORTS = {
     "erp_server_create": (C.c_int, [C.POINTER(ServerParams), C.POINTER(C.c_void_p)]),
     "erp_server_submit": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(Design), C.POINTER(Params)]),
@@ -142,6 +159,16 @@ EXPORTS = {
     "erp_synth_create": (C.c_int, [C.POINTER(SynthParams), C.POINTER(C.c_void_p)]),
     "erp_synth_design": (C.c_int, [C.c_void_p, C.POINTER(Design)]),
     "erp_synth_destroy": (None, [C.c_void_p]),
+    "erp_lefdef_read": (C.c_int, [C.POINTER(C.c_char_p), C.c_int32, C.c_char_p, C.POINTER(C.c_void_p)]),
+    "erp_lefdef_last_error": (C.c_char_p, []),
+    "erp_netlist_design": (C.c_int, [C.c_void_p, C.POINTER(Design)]),
+    "erp_netlist_stats": (C.c_int, [C.c_void_p, C.POINTER(LefDefStats)]),
+    "erp_netlist_node_name": (C.c_char_p, [C.c_void_p, C.c_int32]),
+    "erp_netlist_net_name": (C.c_char_p, [C.c_void_p, C.c_int32]),
+    "erp_netlist_from_design": (C.c_int, [C.POINTER(Design), C.POINTER(LefDefParams), C.POINTER(C.c_void_p)]),
+    "erp_lefdef_write": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
+    "erp_def_write_placed": (C.c_int, [C.c_void_p, f32p, f32p, C.c_char_p]),
+    "erp_netlist_destroy": (None, [C.c_void_p]),
 }
 
 _lib = None
