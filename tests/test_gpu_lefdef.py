@@ -49,7 +49,7 @@ def small_files(R, LD, tmp_path_factory):
     return lef, de, cfg
 
 
-@pytest.mark.parametrize("m,n", [(16, 16), (8, 32)])
+@pytest.mark.parametrize("m,n", [(16, 16), (16, 32)])
 def test_hand_written_design_stages(R, O, LD, m, n):
     d = LD.read_db([TECH, CELLS], DEF)
     xy = spread_positions(d, seed=5, frac=0.6)
