@@ -8,7 +8,10 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
 #include <memory>
+#include <mutex>
 #include <thread>
 #include <string>
 #include <vector>
@@ -1283,6 +1286,7 @@ struct Job {
     int64_t footprint = 0;
     erp_ctx *ctx = nullptr;
     int start_iter = 0;
+    erp_status prep = ERP_OK;   // outcome of the admission worker's set-up
 };
 }  // namespace
 
@@ -1307,10 +1311,67 @@ struct erp_server {
     int32_t *d_done = nullptr, *h_done = nullptr;
     std::chrono::steady_clock::time_point t0;
     std::string err;
+    // Admission workers: a job admitted by the pump (slot and budget reserved)
+    // is set up on a worker thread -- host preparation, uploads on the job's own
+    // stream, graph capture -- and handed back through `ready`; retired
+    // contexts are destroyed there as well, so the pump thread only launches,
+    // retires and admits.
+    std::vector<std::unique_ptr<Job>> preparing;   // owned here while a worker sets it up
+    std::mutex mu;
+    std::condition_variable cv, ready_cv;
+    std::deque<Job *> todo;                        // guarded by mu
+    std::deque<erp_ctx *> to_destroy;              // guarded by mu
+    std::vector<Job *> ready;                      // guarded by mu
+    std::vector<std::thread> workers;
+    bool stop = false;                             // guarded by mu
     double now() const {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
 };
+
+static void server_worker(erp_server *sv) {
+    cudaSetDevice(sv->p.device);
+    for (;;) {
+        Job *j = nullptr;
+        erp_ctx *dead = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(sv->mu);
+            sv->cv.wait(lk, [&] { return sv->stop || !sv->todo.empty() || !sv->to_destroy.empty(); });
+            if (!sv->to_destroy.empty()) {
+                dead = sv->to_destroy.front();
+                sv->to_destroy.pop_front();
+            } else if (!sv->todo.empty()) {
+                j = sv->todo.front();
+                sv->todo.pop_front();
+            } else {
+                return;   // stop, nothing left
+            }
+        }
+        if (dead) {
+            erp_destroy(dead);
+            continue;
+        }
+        erp_status s = erp_create(&j->des->d, &j->prm, &j->ctx);
+        if (s == ERP_OK) {
+            Ctx &c = j->ctx->c;
+            c.h_st->stop_overflow = sv->p.stop_overflow > 0 ? sv->p.stop_overflow : 0.0f;
+            c.h_st->stop_iter = sv->p.max_iterations;
+            c.h_st->done = 0;
+            if (cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream) != cudaSuccess)
+                s = ERP_ECUDA;
+            if (s == ERP_OK) s = ensure_graph(c);
+        } else {
+            j->ctx = nullptr;
+        }
+        j->prep = s;
+        j->des.reset();   // the context holds its own copy
+        {
+            std::lock_guard<std::mutex> lk(sv->mu);
+            sv->ready.push_back(j);
+        }
+        sv->ready_cv.notify_one();
+    }
+}
 
 extern "C" erp_status erp_server_create(const erp_server_params *p, erp_server **out) {
     g_create_err.clear();
@@ -1337,6 +1398,15 @@ extern "C" erp_status erp_server_create(const erp_server_params *p, erp_server *
     if (!ok) {
         erp_server_destroy(sv);
         g_create_err = "server allocation failed";
+        return ERP_ENOMEM;
+    }
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nw = std::max(1, std::min({4, K, (int)(hw ? hw / 2 : 1)}));
+    try {
+        for (int i = 0; i < nw; ++i) sv->workers.emplace_back(server_worker, sv);
+    } catch (...) {
+        erp_server_destroy(sv);
+        g_create_err = "cannot start admission workers";
         return ERP_ENOMEM;
     }
     *out = sv;
@@ -1428,16 +1498,22 @@ static erp_status server_launch_round(erp_server *sv, int buf) {
 
 static void server_bury(erp_server *sv, uint64_t completed_round) {
     std::vector<std::pair<uint64_t, std::unique_ptr<Job>>> keep;
-    for (auto &g : sv->grave) {
-        if (g.first <= completed_round) {
-            erp_destroy(g.second->ctx);
-            g.second->ctx = nullptr;
-            sv->used -= g.second->footprint;
-        } else {
-            keep.push_back(std::move(g));
+    int n = 0;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        for (auto &g : sv->grave) {
+            if (g.first <= completed_round) {
+                sv->to_destroy.push_back(g.second->ctx);   // freed on a worker (stream-ordered)
+                g.second->ctx = nullptr;
+                sv->used -= g.second->footprint;
+                ++n;
+            } else {
+                keep.push_back(std::move(g));
+            }
         }
     }
     sv->grave.swap(keep);
+    if (n) sv->cv.notify_all();
 }
 
 extern "C" erp_status erp_server_pump(erp_server *sv, int32_t *active_out, int32_t *queued_out) {
@@ -1479,8 +1555,39 @@ extern "C" erp_status erp_server_pump(erp_server *sv, int32_t *active_out, int32
     }
     if (!launched && !sv->round_pending[cur] && !sv->round_pending[prev])
         server_bury(sv, sv->rounds_launched);   // idle: everything launched has completed
-    // 3. admission: FIFO while the job fits the budget and a slot is free
-    while (sv->qhead < sv->queue.size() && (int)sv->active.size() < sv->p.max_active) {
+    // 3. jobs the admission workers have finished setting up join the next round
+    //    (when nothing runs, wait briefly for one instead of spinning)
+    std::vector<Job *> got;
+    {
+        std::unique_lock<std::mutex> lk(sv->mu);
+        if (sv->ready.empty() && sv->active.empty() && !sv->preparing.empty() && !sv->round_pending[0] &&
+            !sv->round_pending[1])
+            sv->ready_cv.wait_for(lk, std::chrono::milliseconds(2), [&] { return !sv->ready.empty(); });
+        got.swap(sv->ready);
+    }
+    for (Job *jr : got) {
+        auto it = std::find_if(sv->preparing.begin(), sv->preparing.end(),
+                               [&](const std::unique_ptr<Job> &p) { return p.get() == jr; });
+        std::unique_ptr<Job> jp = std::move(*it);
+        sv->preparing.erase(it);
+        if (jp->prep != ERP_OK) {
+            server_record(sv, *jp, jp->prep);
+            if (jp->ctx) {
+                std::lock_guard<std::mutex> lk(sv->mu);
+                sv->to_destroy.push_back(jp->ctx);
+                jp->ctx = nullptr;
+            }
+            sv->cv.notify_one();
+            sv->used -= jp->footprint;
+            continue;
+        }
+        jp->start_iter = 0;
+        sv->active.push_back(std::move(jp));
+    }
+    // 4. admission: FIFO while the job fits the budget and a slot is free; the
+    //    set-up itself runs on a worker
+    int admitted = 0;
+    while (sv->qhead < sv->queue.size() && (int)(sv->active.size() + sv->preparing.size()) < sv->p.max_active) {
         Job &j = *sv->queue[sv->qhead];
         if (j.footprint > sv->p.hbm_budget_bytes) {   // can never fit
             std::unique_ptr<Job> jp = std::move(sv->queue[sv->qhead++]);
@@ -1489,29 +1596,22 @@ extern "C" erp_status erp_server_pump(erp_server *sv, int32_t *active_out, int32
         }
         if (sv->used + j.footprint > sv->p.hbm_budget_bytes) break;
         std::unique_ptr<Job> jp = std::move(sv->queue[sv->qhead++]);
-        erp_status s = erp_create(&jp->des->d, &jp->prm, &jp->ctx);
         jp->admit = sv->now();
-        if (s != ERP_OK) {
-            jp->ctx = nullptr;
-            server_record(sv, *jp, s);
-            continue;
-        }
-        Ctx &c = jp->ctx->c;
-        c.h_st->stop_overflow = sv->p.stop_overflow > 0 ? sv->p.stop_overflow : 0.0f;
-        c.h_st->stop_iter = sv->p.max_iterations;
-        c.h_st->done = 0;
-        cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream);
-        jp->start_iter = 0;
         sv->used += jp->footprint;
-        jp->des.reset();   // the context holds its own copy
-        sv->active.push_back(std::move(jp));
+        {
+            std::lock_guard<std::mutex> lk(sv->mu);
+            sv->todo.push_back(jp.get());
+        }
+        sv->preparing.push_back(std::move(jp));
+        ++admitted;
     }
+    if (admitted) sv->cv.notify_all();
     if (sv->qhead > 1024 && sv->qhead * 2 > sv->queue.size()) {   // compact the FIFO
         sv->queue.erase(sv->queue.begin(), sv->queue.begin() + sv->qhead);
         sv->qhead = 0;
     }
     if (launched) sv->round ^= 1;
-    if (active_out) *active_out = (int32_t)sv->active.size();
+    if (active_out) *active_out = (int32_t)(sv->active.size() + sv->preparing.size());
     if (queued_out) *queued_out = (int32_t)(sv->queue.size() - sv->qhead);
     return ERP_OK;
 }
@@ -1543,12 +1643,22 @@ extern "C" const char *erp_server_last_error(const erp_server *sv) { return sv ?
 
 extern "C" void erp_server_destroy(erp_server *sv) {
     if (!sv) return;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->todo.clear();   // not started: nothing to undo
+        sv->stop = true;
+    }
+    sv->cv.notify_all();
+    for (auto &t : sv->workers) t.join();   // a worker finishes its pending destroys first
     cudaSetDevice(sv->p.device);
     if (sv->master) cudaStreamSynchronize(sv->master);
     for (auto &j : sv->active)
         if (j->ctx) erp_destroy(j->ctx);
+    for (auto &j : sv->preparing)
+        if (j->ctx) erp_destroy(j->ctx);
     for (auto &g : sv->grave)
         if (g.second->ctx) erp_destroy(g.second->ctx);
+    for (auto *c : sv->to_destroy) erp_destroy(c);
     for (auto e : sv->job_ev)
         if (e) cudaEventDestroy(e);
     for (auto e : sv->round_ev)
