@@ -497,7 +497,7 @@ static void enqueue_potential(Ctx &c, bool stage, bool want_psi) {
     if (stage || c.map_dirty) cudaMemsetAsync(c.dmap, 0, sizeof(unsigned long long) * (size_t)c.m * c.n, c.stream);
     launch_density_scatter(c);
     launch_spectral(c, /*zero_map=*/!stage, /*store_rho=*/stage, want_psi);
-    launch_force(c);
+    launch_force(c, 0);
     c.map_dirty = stage;
 }
 
@@ -550,7 +550,7 @@ void enqueue_step_kernels(Ctx &c) {
     launch_wl_gather(c);
     launch_density_scatter(c);
     launch_spectral(c, /*zero_map=*/true, /*store_rho=*/false, /*want_psi=*/false);
-    launch_force(c);
+    launch_force(c, 1);
     launch_nesterov(c, -1);
     launch_scheduler(c, 0, 0.f, 0.f);
 }
@@ -826,7 +826,7 @@ extern "C" erp_status erp_profile_stages(erp_ctx *ctx, int32_t reps, float *ms_o
                 launch_density_scatter(c);
                 break;
             case ERP_STAGE_SPECTRAL: launch_spectral(c, true, false, false); break;
-            case ERP_STAGE_FORCE: launch_force(c); break;
+            case ERP_STAGE_FORCE: launch_force(c, 1); break;
             case ERP_STAGE_NESTEROV: launch_nesterov(c, -1); break;
             default: launch_scheduler(c, 0, 0.f, 0.f); break;
             }

@@ -134,7 +134,7 @@ void launch_initial_density(Ctx &c, const float *hx, const float *hy, const floa
                             const float *hh);               // setup, on device
 void launch_density_scatter(Ctx &c);
 void launch_spectral(Ctx &c, bool zero_map, bool store_rho, bool want_psi);
-void launch_force(Ctx &c);
+void launch_force(Ctx &c, int rescale);                   // rescale 1: also the iteration-0 density-weight rescale (step graph)
 void launch_energy(Ctx &c);
 // optimiser + scheduler (src/nesterov.rs, src/scheduler.rs)
 void launch_nesterov(Ctx &c, int iter_arg);                // iter_arg < 0: read DevState.iteration

@@ -230,7 +230,7 @@ struct WaClasses {
     int block0[kNumClasses + 1];
 };
 
-__global__ void __launch_bounds__(kThreads, 3) k_wa(WaArgs a, WaClasses cl, float gamma_arg,
+__global__ void __launch_bounds__(kThreads, 4) k_wa(WaArgs a, WaClasses cl, float gamma_arg,
                                                  double *__restrict__ partials, DevState *st) {
     __shared__ double shr[kThreads / 32];
     if (st->done) return;
@@ -507,8 +507,15 @@ __global__ void __launch_bounds__(kThreads) k_force(
     const float *__restrict__ ch, const float *__restrict__ ratio, int m, int n, float bw,
     float bh, float inv_bw, float inv_bh, const float *__restrict__ fx,
     const float *__restrict__ fy, float *__restrict__ gx_out, float *__restrict__ gy_out,
-    const DevState *__restrict__ st) {
+    int rescale, const float *__restrict__ wlgx, const float *__restrict__ wlgy,
+    double *__restrict__ partials, DevState *st) {
+    __shared__ double shr[kThreads / 32];
     if (st->done) return;
+    // Inside the step graph (rescale = 1) the iteration-0 density-weight rescale
+    // (src/nesterov.rs:47-55) rides on this pass: the WA gradient is complete and
+    // the density gradient is produced here, so no extra launch per step.
+    const bool do_rescale = rescale && st->iteration == 0;   // grid-uniform
+    double sa = 0.0, sb = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
         const float sx = cw[i], sy = ch[i];
         const float nx = x[i] + offx[i], ny = y[i] + offy[i], r = ratio[i];
@@ -533,6 +540,27 @@ __global__ void __launch_bounds__(kThreads) k_force(
         }
         gx_out[i] = -gx * r;
         gy_out[i] = -gy * r;
+    }
+    if (do_rescale) {
+        // a loop of its own: FP64 work predicated inside the loop above would
+        // occupy the FP64 pipe on every step, not only at iteration 0
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
+            sa += (double)fabsf(wlgx[i]) + (double)fabsf(wlgy[i]);
+            sb += (double)fabsf(gx_out[i]) + (double)fabsf(gy_out[i]);   // written by this thread above
+        }
+        double vals[2];
+        vals[0] = block_sum(sa, shr);
+        vals[1] = block_sum(sb, shr);
+        if (arrive_last(partials, blockIdx.x, 2, vals, &st->ctr[CTR_ABS], gridDim.x)) {
+            const double num = sum_partials(partials, gridDim.x, 2, 0, shr);
+            const double den = sum_partials(partials, gridDim.x, 2, 1, shr);
+            if (threadIdx.x == 0) {
+                st->abs_wl = num;
+                st->abs_dens = den;
+                st->dw = (float)((double)st->dw * (num / den));
+                st->ctr[CTR_ABS] = 0;
+            }
+        }
     }
 }
 
@@ -746,10 +774,34 @@ __global__ void k_pack_xy(int N, const float *__restrict__ x, const float *__res
 // Scheduler::update + should_stop (src/scheduler.rs:68-130) in FP64, plus the
 // step record, the non-finite check and the retire-at-overflow flag.
 __global__ void k_scheduler(int use_args, float hpwl_arg, float ovf_arg, DevState *st) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    if (st->done) return;
+    if (blockIdx.x != 0) return;
+    if (st->done) return;   // warp-uniform
     const float hpwl = use_args ? hpwl_arg : st->hpwl_f;
     const float ovf = use_args ? ovf_arg : st->overflow_f;
+    // The density-weight power (lane 0) and the gamma coefficient (lane 1) are
+    // independent FP64 powers: one convergent pow call evaluates both, with the
+    // same arguments as two calls in sequence and so the same results.
+    const int lane = threadIdx.x & 31;
+    const int it1 = st->iteration + 1;
+    const float ref0 = st->hpwl_init_set ? st->hpwl_init : hpwl;
+    const float delta0 = hpwl - st->hpwl_cur;   // hpwl_cur - hpwl_prev after the update below
+    double base, ex;
+    if (lane == 1) {
+        base = 10.0;
+        ex = ((double)ovf - 0.1) * 20.0 / 9.0 - 1.0;
+    } else if (delta0 < 0.0f) {
+        base = 0.9999;
+        ex = (double)it1;
+    } else {
+        base = 1.05;
+        ex = -(double)delta0 / (double)ref0;
+    }
+    double pw = pow(base, ex);
+    if (lane == 1) pw = pw < 0.05 ? 0.05 : (pw > 10.0 ? 10.0 : pw);
+    else if (delta0 < 0.0f) pw = pw < 0.98 ? 0.98 : pw;
+    else pw = pw < 0.95 ? 0.95 : (pw > 1.05 ? 1.05 : pw);
+    const double coef_l1 = __shfl_sync(0xffffffffu, pw, 1);
+    if (lane != 0) return;
     erp_step_stats rec;
     rec.iteration = st->iteration;
     rec.hpwl = hpwl;
@@ -763,20 +815,9 @@ __global__ void k_scheduler(int use_args, float hpwl_arg, float ovf_arg, DevStat
     if (!st->ovf_init_set) { st->ovf_init = ovf; st->ovf_init_set = 1; }
     st->ovf_prev = st->ovf_cur;
     st->ovf_cur = ovf;
-    const float ref = st->hpwl_init;
-    const float delta = st->hpwl_cur - st->hpwl_prev;
-    double power;
-    if (delta < 0.0f) {
-        power = pow(0.9999, (double)st->iteration);
-        if (power < 0.98) power = 0.98;
-    } else {
-        power = pow(1.05, -(double)delta / (double)ref);
-        power = power < 0.95 ? 0.95 : (power > 1.05 ? 1.05 : power);
-    }
+    const double power = pw;   // the rule above, on hpwl_init / hpwl_cur - hpwl_prev / iteration as updated here
     st->dw = (float)((double)st->dw * (1.05 * power));
-    double coef = pow(10.0, ((double)st->ovf_cur - 0.1) * 20.0 / 9.0 - 1.0);
-    coef = coef < 0.05 ? 0.05 : (coef > 10.0 ? 10.0 : coef);
-    st->gamma = (float)((double)st->base_gamma * coef);
+    st->gamma = (float)((double)st->base_gamma * coef_l1);
     const float cur = st->hpwl_cur, prev = st->hpwl_prev;
     rec.should_stop = (prev != 0.0f && cur != 0.0f && prev > cur * 1.5f) ? 1 : 0;
     rec.alpha = st->alpha;
@@ -895,10 +936,10 @@ void launch_initial_density(Ctx &c, const float *, const float *, const float *,
         mn, c.dmap, ldexpf(1.0f, -c.shift0), c.target_density, c.initial);
 }
 
-void launch_force(Ctx &c) {
+void launch_force(Ctx &c, int rescale) {
     k_force<<<grid_for(c.NM, 152 * 16), kThreads, 0, c.stream>>>(
         c.NM, c.x, c.y, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw,
-        c.inv_bh, c.fx, c.fy, c.dgx, c.dgy, c.st);
+        c.inv_bh, c.fx, c.fy, c.dgx, c.dgy, rescale, c.wlgx, c.wlgy, c.partials, c.st);
 }
 
 void launch_energy(Ctx &c) {
@@ -908,9 +949,11 @@ void launch_energy(Ctx &c) {
 }
 
 void launch_nesterov(Ctx &c, int iter_arg) {
-    const int g = grid_for(c.NM);
-    k_dw_rescale<<<g, kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx, c.dgy,
-                                               c.partials, c.st);
+    if (iter_arg >= 0) {   // stage entry point; in the step graph k_force does the rescale
+        const int g = grid_for(c.NM);
+        k_dw_rescale<<<g, kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx, c.dgy,
+                                                   c.partials, c.st);
+    }
     const int g4 = grid_for((c.NM + 3) / 4);
     k_nesterov_grad<<<g4, kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx, c.dgy, c.w,
                                                   c.h, c.npins, c.x, c.y, c.prev_x, c.prev_y,
