@@ -305,11 +305,15 @@ typedef enum erp_stage {
     ERP_STAGE_WL_GATHER = 1,  /* instance gradients from the pin gradients */
     ERP_STAGE_DENSITY = 2,    /* map clear + density scatter */
     ERP_STAGE_SPECTRAL = 3,   /* map conversion + overflow + Poisson solve (3 passes) */
-    ERP_STAGE_FORCE = 4,      /* electric force gather */
-    ERP_STAGE_NESTEROV = 5,   /* rescale + preconditioned gradient / Lipschitz + update */
+    ERP_STAGE_FORCE = 4,      /* electric force gather (+ the iteration-0 density-weight rescale) */
+    ERP_STAGE_NESTEROV = 5,   /* preconditioned gradient / Lipschitz + update */
     ERP_STAGE_SCHEDULER = 6,
     ERP_NUM_STAGES = 7
 } erp_stage;
+/* reps > 0: each stage alone, L2 flushed before every launch (mutates the
+ * state).  reps < 0: -reps whole steps launched in graph order with an event
+ * between the stages and warm caches (advances the placement by -reps + 1
+ * iterations).  ms_out receives ERP_NUM_STAGES mean milliseconds. */
 erp_status erp_profile_stages(erp_ctx *ctx, int32_t reps, float *ms_out);
 
 /* ---- standalone spectral solve (the Poisson part of compute_potential,

@@ -154,7 +154,8 @@ void free_ctx(Ctx &c) {
                     c.dgx, c.dgy, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.slot_cell, c.slot_off,
                     c.slot_grad, c.net_ptr, c.net_hpwl, c.cell_slot_ptr, c.cell_slots, c.dmap,
                     c.initial, c.rho, c.t1, c.tx, c.ty, c.tp, c.fx, c.fy, c.psi, c.tw_m, c.tw_n,
-                    c.ek_m, c.ek_n, c.wu, c.wv, c.partials, c.st};
+                    c.ek_m, c.ek_n, c.wu, c.wv, c.partials, c.st, c.perm, c.skey, c.soff, c.sratio,
+                    c.sort_key, c.sort_rank, c.sort_hist, c.sort_start};
     for (void *p : ptrs) {   // stream-ordered, on the stream they were allocated on
         if (!p) continue;
         if (c.stream) cudaFreeAsync(p, c.stream);
@@ -373,6 +374,14 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     CK(dalloc(&c.net_hpwl, E, s0));
     CK(dalloc(&c.cell_slot_ptr, (size_t)NM + 1, s0));
     CK(dalloc(&c.cell_slots, hcell_slots.size(), s0));
+    CK(dalloc(&c.perm, NM, s0));
+    CK(dalloc(&c.skey, NM, s0));
+    CK(dalloc(&c.soff, NM, s0));
+    CK(dalloc(&c.sratio, NM, s0));
+    CK(dalloc(&c.sort_key, NM, s0));
+    CK(dalloc(&c.sort_rank, NM, s0));
+    CK(dalloc(&c.sort_hist, scatter_tiles(c.m, c.n), s0));
+    CK(dalloc(&c.sort_start, scatter_tiles(c.m, c.n), s0));
     CK(dalloc(&c.dmap, mn, s0));
     float **maps[] = {&c.initial, &c.rho, &c.t1, &c.tx, &c.ty, &c.tp, &c.fx, &c.fy, &c.psi};
     for (float **a : maps) CK(dalloc(a, mn, s0));
@@ -422,6 +431,8 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     *c.h_st = h;
     CK(cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream));
     launch_pack_xy(c);
+    launch_scatter_order(c, c.stream);
+    c.sort_age = 0;
     // fixed-cell initial density (src/epotential.rs:127-140)
     launch_initial_density(c, nullptr, nullptr, nullptr, nullptr);
     CK(cudaGetLastError());
@@ -591,9 +602,20 @@ static erp_status ensure_graph(Ctx &c) {
     return ERP_OK;
 }
 
+// The scatter order follows the cells every kSortEvery steps (a stale order is
+// still correct, only slower).
+static void refresh_scatter_order(Ctx &c, int steps, cudaStream_t s) {
+    c.sort_age += steps;
+    if (c.sort_age >= kSortEvery) {
+        launch_scatter_order(c, s);
+        c.sort_age = 0;
+    }
+}
+
 static erp_status enqueue_step(Ctx &c) {
     erp_status s = ensure_graph(c);
     if (s != ERP_OK) return s;
+    refresh_scatter_order(c, 1, c.stream);
     if (c.map_dirty) {
         CK(cudaMemsetAsync(c.dmap, 0, sizeof(unsigned long long) * (size_t)c.m * c.n, c.stream));
         c.map_dirty = false;
@@ -802,9 +824,54 @@ extern "C" erp_status erp_synchronize(erp_ctx *ctx) {
     return ERP_OK;
 }
 
+// reps < 0: -reps whole steps launched eagerly in graph order with an event
+// between the stages and no flush (warm caches, as inside the step graph).
+static erp_status profile_warm(Ctx &c, int reps, float *ms_out) {
+    cudaEvent_t ev[ERP_NUM_STAGES + 1];
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    if (c.map_dirty) {
+        CK(cudaMemsetAsync(c.dmap, 0, sizeof(unsigned long long) * (size_t)c.m * c.n, c.stream));
+        c.map_dirty = false;
+    }
+    double tot[ERP_NUM_STAGES] = {0};
+    erp_status rc = ERP_OK;
+    for (int r = 0; r <= reps && rc == ERP_OK; ++r) {   // r == 0: untimed warm-up
+        cudaEventRecord(ev[0], c.stream);
+        launch_wirelength(c, -1.0f);
+        cudaEventRecord(ev[1], c.stream);
+        launch_wl_gather(c);
+        cudaEventRecord(ev[2], c.stream);
+        launch_density_scatter(c);
+        cudaEventRecord(ev[3], c.stream);
+        launch_spectral(c, /*zero_map=*/true, false, false);
+        cudaEventRecord(ev[4], c.stream);
+        launch_force(c, 1);
+        cudaEventRecord(ev[5], c.stream);
+        launch_nesterov(c, -1);
+        cudaEventRecord(ev[6], c.stream);
+        launch_scheduler(c, 0, 0.f, 0.f);
+        cudaEventRecord(ev[7], c.stream);
+        const cudaError_t err = cudaEventSynchronize(ev[7]);
+        if (err != cudaSuccess) {
+            c.err = cudaGetErrorString(err);
+            rc = ERP_ECUDA;
+            break;
+        }
+        for (int k = 0; k < ERP_NUM_STAGES && r > 0; ++k) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+            tot[k] += ms;
+        }
+    }
+    for (int k = 0; k < ERP_NUM_STAGES; ++k) ms_out[k] = (float)(tot[k] / reps);
+    for (auto &e : ev) cudaEventDestroy(e);
+    return rc;
+}
+
 extern "C" erp_status erp_profile_stages(erp_ctx *ctx, int32_t reps, float *ms_out) {
     CTX_CHECK();
-    if (reps < 1 || !ms_out) return ERP_EINVAL;
+    if (reps == 0 || !ms_out) return ERP_EINVAL;
+    if (reps < 0) return profile_warm(c, -reps, ms_out);
     const size_t flush_bytes = 256u << 20;
     void *flush = nullptr;
     CK(cudaMalloc(&flush, flush_bytes));
@@ -1155,6 +1222,8 @@ extern "C" erp_status erp_batch_run(erp_batch *b, int32_t max_iterations, float 
     erp_status rs = ERP_OK;
     while (n_active > 0 && launched < max_iterations) {
         const int k = std::min(chunk, max_iterations - launched);
+        for (int i = 0; i < K; ++i)
+            if (active[i]) refresh_scatter_order(b->ctx[i]->c, k, b->master);
         for (int i = 0; i < k && rs == ERP_OK; ++i)
             if (cudaGraphLaunch(b->graph, b->master) != cudaSuccess)
                 rs = batch_fail(b, ERP_ECUDA, "batch graph launch failed");
@@ -1246,6 +1315,7 @@ extern "C" erp_status erp_estimate_footprint(const erp_design *d, const erp_para
     int64_t b = 18 * al(4 * (N + 4));
     b += al(4 * P) + 2 * al(8 * P) + al(4 * (E + 1)) + al(4 * E) + al(4 * (NM + 1)) + al(4 * movable_pins);
     b += al(8 * mn) + 9 * al(4 * mn) + al(8 * (int64_t)kMaxPartials) + al(sizeof(DevState));
+    b += 5 * al(4 * (int64_t)NM) + al(16 * (int64_t)NM) + 2 * al(4 * (int64_t)scatter_tiles(m, n));   // scatter order
     b += al(8 * (m / 2)) + al(8 * (n / 2)) + al(8 * m) + al(8 * n) + al(4 * m) + al(4 * n);
     if (pp && pp->precision != ERP_PREC_FP32) {   // tensor-core plan: 4 transforms per axis + 7 map buffers
         const int64_t es = pp->precision == ERP_PREC_TF32_GEMM ? 4 : 4;   // fp32, or bf16 hi + lo
@@ -1476,6 +1546,7 @@ static erp_status server_launch_round(erp_server *sv, int buf) {
             sv->err = c.err;
             return s;
         }
+        refresh_scatter_order(c, sv->p.chunk, c.stream);
         for (int k = 0; k < sv->p.chunk; ++k)
             if (cudaGraphLaunch(c.graph, c.stream) != cudaSuccess) {
                 sv->err = "job graph launch failed";

@@ -96,6 +96,12 @@ struct Ctx {
     NetClass cls[kNumClasses];
     int32_t *cell_slot_ptr;    // [NM+1]
     int32_t *cell_slots;
+    // --- scatter order [NM] (k_density_scatter; refreshed every kSortEvery steps) ---
+    int32_t *perm, *skey;      // cell at each scatter position, its sort tile
+    float4 *soff;              // offx, offy, cw, ch in scatter order
+    float *sratio;
+    int32_t *sort_key, *sort_rank, *sort_hist, *sort_start;   // counting-sort scratch ([NM], [NM], tiles, tiles)
+    int32_t sort_age;          // steps since the order was computed
     // host-side permutations for test hooks
     int32_t *h_slot_of_pin;    // [P]
     int32_t *h_net_of_internal;// [E]
@@ -134,6 +140,9 @@ void launch_initial_density(Ctx &c, const float *hx, const float *hy, const floa
                             const float *hh);               // setup, on device
 void launch_density_scatter(Ctx &c);
 void launch_spectral(Ctx &c, bool zero_map, bool store_rho, bool want_psi);
+void launch_scatter_order(Ctx &c, cudaStream_t s);   // recompute the scatter order from the current positions
+int scatter_tiles(int m, int n);
+constexpr int kSortEvery = 16;                          // steps between scatter-order refreshes
 void launch_force(Ctx &c, int rescale);                   // rescale 1: also the iteration-0 density-weight rescale (step graph)
 void launch_energy(Ctx &c);
 // optimiser + scheduler (src/nesterov.rs, src/scheduler.rs)

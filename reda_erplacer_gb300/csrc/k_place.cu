@@ -330,15 +330,25 @@ __device__ __forceinline__ float tri_clamped(float x, float s, int k, float bs) 
 //    edge -- cost one global atomic per block.
 // Early on all cells sit within a few bins of the die centre, where this turns
 // millions of contended global atomics into a few per block.
+//
+// Cells are taken in the scatter order (perm, refreshed every few steps by
+// launch_scatter_order): movable cells counting-sorted by a kSortTile-bin square
+// tile of their position, so a block's cells share a tile and its window sits
+// on that tile with kSortPad bins of slack on each side.  Positions come from
+// the packed xy array; the stretched offsets, sizes and ratios were gathered
+// into the scatter order when it was computed (they never change).  Any
+// permutation gives the same integer sums: the order only decides how many
+// contributions find the window.
 constexpr int kWin = 64;
+constexpr int kSortTile = 48, kSortPad = 8;
+static_assert(kSortTile + 2 * kSortPad == kWin, "the window covers a tile and its pads");
 constexpr int kTableLog = 9, kTable = 1 << kTableLog;   // out-of-window bin table (open, no probing)
 constexpr unsigned kEmpty = 0xffffffffu;                 // bin indices are < 4096 * 4096
 constexpr int kMaxCellsPerBlock = 2048;
 constexpr unsigned long long kPiece = (1ull << 21) - 1;
 __global__ void __launch_bounds__(kThreads) k_density_scatter(
-    int NM, const float *__restrict__ x, const float *__restrict__ y,
-    const float *__restrict__ offx, const float *__restrict__ offy, const float *__restrict__ cw,
-    const float *__restrict__ ch, const float *__restrict__ ratio, int m, int n, float bw,
+    int NM, const int32_t *__restrict__ perm, const float2 *__restrict__ xy, const float4 *__restrict__ soff,
+    const float *__restrict__ sratio, const int32_t *__restrict__ skey, int nty, int m, int n, float bw,
     float bh, float inv_bw, float inv_bh, float scale, unsigned long long *__restrict__ map,
     const DevState *__restrict__ st) {
     extern __shared__ unsigned dsm[];
@@ -348,10 +358,11 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
     if (st->done) return;
     const int per = ((NM + gridDim.x - 1) / gridDim.x + 31) & ~31;   // <= kMaxCellsPerBlock (launcher)
     const int c0 = blockIdx.x * per, c1 = min(c0 + per, NM);
-    int wox = 0, woy = 0;   // window origin: every thread derives it from the block's first cell
+    int wox = 0, woy = 0;   // window origin: the sort tile of the block's first cell, less the pad
     if (c0 < NM) {
-        wox = (int)floorf(clamp_bin((x[c0] + offx[c0]) * inv_bw, m)) - kWin / 2;
-        woy = (int)floorf(clamp_bin((y[c0] + offy[c0]) * inv_bh, n)) - kWin / 2;
+        const int k0 = skey[c0];
+        wox = (k0 / nty) * kSortTile - kSortPad;
+        woy = (k0 % nty) * kSortTile - kSortPad;
     }
     wox = max(0, min(wox, m - kWin));
     woy = max(0, min(woy, n - kWin));
@@ -360,15 +371,17 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
     for (int k = threadIdx.x; k < 3 * kTable; k += blockDim.x) tplane[k] = 0u;
     __syncthreads();
     for (int base = c0; base < c1; base += blockDim.x) {
-        const int i = base + threadIdx.x;
+        const int p = base + threadIdx.x;
         int bxl = 0, byl = 0, nx = 0, ny = 0;
         float xi = 0.f, yi = 0.f, sxi = 0.f, syi = 0.f, r = 0.f;
-        if (i < c1) {
-            xi = x[i] + offx[i];
-            yi = y[i] + offy[i];
-            sxi = cw[i];
-            syi = ch[i];
-            r = ratio[i];
+        if (p < c1) {
+            const float2 q = xy[perm[p]];
+            const float4 o = soff[p];   // offx, offy, cw, ch of cell perm[p]
+            xi = q.x + o.x;
+            yi = q.y + o.y;
+            sxi = o.z;
+            syi = o.w;
+            r = sratio[p];
             int xl = (int)floorf(clamp_bin((xi - 0.0f) * inv_bw, m));
             int xh = (int)ceilf(clamp_bin((xi - 0.0f + sxi) * inv_bw, m)) + 1;
             int yl = (int)floorf(clamp_bin((yi - 0.0f) * inv_bh, n));
@@ -437,6 +450,95 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
 }
 
 size_t density_scatter_smem() { return sizeof(unsigned) * (3 * kWin * kWin + 4 * kTable); }
+
+// Scatter order: counting sort of the movable cells by sort tile.  Ranks within
+// a tile follow atomic order (any order is valid, see k_density_scatter).
+__global__ void __launch_bounds__(kThreads) k_sort_count(int NM, const float2 *__restrict__ xy,
+                                                         const float *__restrict__ offx,
+                                                         const float *__restrict__ offy, float inv_bw,
+                                                         float inv_bh, int m, int n, int nty, int ntiles,
+                                                         int32_t *__restrict__ key, int32_t *__restrict__ rank,
+                                                         int32_t *__restrict__ hist) {
+    extern __shared__ int32_t tcount[];   // per tile: the block's count, then its base in the tile
+    constexpr int PER = 4;
+    for (int k = threadIdx.x; k < ntiles; k += blockDim.x) tcount[k] = 0;
+    __syncthreads();
+    int kk[PER], rr[PER];
+    const int base = blockIdx.x * blockDim.x * PER;
+#pragma unroll
+    for (int t = 0; t < PER; ++t) {
+        const int i = base + t * blockDim.x + threadIdx.x;
+        kk[t] = -1;
+        rr[t] = 0;
+        if (i < NM) {
+            const float2 q = xy[i];
+            int bx = (int)floorf(clamp_bin((q.x + offx[i]) * inv_bw, m));
+            int by = (int)floorf(clamp_bin((q.y + offy[i]) * inv_bh, n));
+            bx = max(0, min(bx, m - 1));
+            by = max(0, min(by, n - 1));
+            kk[t] = (bx / kSortTile) * nty + by / kSortTile;
+            rr[t] = atomicAdd(tcount + kk[t], 1);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < ntiles; k += blockDim.x) {
+        const int v = tcount[k];
+        if (v) tcount[k] = atomicAdd(hist + k, v);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < PER; ++t) {
+        const int i = base + t * blockDim.x + threadIdx.x;
+        if (kk[t] >= 0) {
+            key[i] = kk[t];
+            rank[i] = tcount[kk[t]] + rr[t];
+        }
+    }
+}
+
+// exclusive prefix sum of the tile counts (one block)
+__global__ void __launch_bounds__(1024) k_sort_scan(int ntiles, const int32_t *__restrict__ hist,
+                                                    int32_t *__restrict__ start) {
+    __shared__ int32_t part[1024];
+    const int per = (ntiles + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(b + per, ntiles);
+    int32_t sum = 0;
+    for (int k = b; k < e; ++k) sum += hist[k];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+        const int32_t v = (int)threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+    for (int k = b; k < e; ++k) {
+        start[k] = run;
+        run += hist[k];
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_sort_place(int NM, const int32_t *__restrict__ key,
+                                                         const int32_t *__restrict__ rank,
+                                                         const int32_t *__restrict__ start,
+                                                         const float *__restrict__ offx,
+                                                         const float *__restrict__ offy,
+                                                         const float *__restrict__ cw, const float *__restrict__ ch,
+                                                         const float *__restrict__ ratio, int32_t *__restrict__ perm,
+                                                         float4 *__restrict__ soff, float *__restrict__ sratio,
+                                                         int32_t *__restrict__ skey) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
+        const int k = key[i];
+        const int p = start[k] + rank[i];
+        perm[p] = i;
+        soff[p] = make_float4(offx[i], offy[i], cw[i], ch[i]);
+        sratio[p] = ratio[i];
+        skey[p] = k;
+    }
+}
+
+int scatter_tiles(int m, int n) { return ((m + kSortTile - 1) / kSortTile) * ((n + kSortTile - 1) / kSortTile); }
 
 cudaError_t place_prepare() {
     return cudaFuncSetAttribute(k_density_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -899,9 +1001,23 @@ void launch_wl_gather(Ctx &c) {
 
 void launch_density_scatter(Ctx &c) {
     const int g = std::max(grid_for(c.NM, 152 * 4), (c.NM + kMaxCellsPerBlock - 1) / kMaxCellsPerBlock);
+    const int nty = (c.n + kSortTile - 1) / kSortTile;
     k_density_scatter<<<g, kThreads, density_scatter_smem(), c.stream>>>(
-        c.NM, c.x, c.y, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw,
+        c.NM, c.perm, c.xy, c.soff, c.sratio, c.skey, nty, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw,
         c.inv_bh, c.fixed_scale, c.dmap, c.st);
+}
+
+void launch_scatter_order(Ctx &c, cudaStream_t s) {
+    if (c.NM <= 0) return;
+    const int nty = (c.n + kSortTile - 1) / kSortTile;
+    const int ntiles = scatter_tiles(c.m, c.n);
+    cudaMemsetAsync(c.sort_hist, 0, sizeof(int32_t) * ntiles, s);
+    k_sort_count<<<(c.NM + 4 * kThreads - 1) / (4 * kThreads), kThreads, sizeof(int32_t) * ntiles, s>>>(
+        c.NM, c.xy, c.offx, c.offy, c.inv_bw, c.inv_bh, c.m, c.n, nty, ntiles, c.sort_key, c.sort_rank,
+        c.sort_hist);
+    k_sort_scan<<<1, 1024, 0, s>>>(ntiles, c.sort_hist, c.sort_start);
+    k_sort_place<<<grid_for(c.NM), kThreads, 0, s>>>(c.NM, c.sort_key, c.sort_rank, c.sort_start, c.offx, c.offy,
+                                                     c.cw, c.ch, c.ratio, c.perm, c.soff, c.sratio, c.skey);
 }
 
 void launch_initial_density(Ctx &c, const float *, const float *, const float *, const float *) {

@@ -117,11 +117,13 @@ class Placement:
     def synchronize(self):
         self._ck(self.lib.erp_synchronize(self.h))
 
-    def profile_stages(self, reps=10):
+    def profile_stages(self, reps=10, warm=False):
         """Mean milliseconds per launch of each stage, timed in isolation with an
-        L2 flush before every launch (mutates the placement state)."""
+        L2 flush before every launch (mutates the placement state); warm=True:
+        whole steps in graph order with events between the stages, caches warm
+        (advances the placement by reps + 1 iterations)."""
         out = (C.c_float * len(L.STAGES))()
-        self._ck(self.lib.erp_profile_stages(self.h, int(reps), out))
+        self._ck(self.lib.erp_profile_stages(self.h, -int(reps) if warm else int(reps), out))
         return dict(zip(L.STAGES, [float(v) for v in out]))
 
     # -- state --
