@@ -604,23 +604,17 @@ __device__ __forceinline__ long long to_isize0(float v) {
 
 // compute_electric_force (src/eforce.rs:15-91)
 __global__ void __launch_bounds__(kThreads) k_force(
-    int NM, const float *__restrict__ x, const float *__restrict__ y,
-    const float *__restrict__ offx, const float *__restrict__ offy, const float *__restrict__ cw,
-    const float *__restrict__ ch, const float *__restrict__ ratio, int m, int n, float bw,
-    float bh, float inv_bw, float inv_bh, const float *__restrict__ fx,
+    int NM, const int32_t *__restrict__ perm, const float2 *__restrict__ xy, const float4 *__restrict__ soff,
+    const float *__restrict__ sratio, const float *__restrict__ offx, const float *__restrict__ offy,
+    const float *__restrict__ cw, const float *__restrict__ ch, const float *__restrict__ ratio, int m, int n,
+    float bw, float bh, float inv_bw, float inv_bh, const float *__restrict__ fx,
     const float *__restrict__ fy, float *__restrict__ gx_out, float *__restrict__ gy_out,
     int rescale, const float *__restrict__ wlgx, const float *__restrict__ wlgy,
     double *__restrict__ partials, DevState *st) {
     __shared__ double shr[kThreads / 32];
     if (st->done) return;
-    // Inside the step graph (rescale = 1) the iteration-0 density-weight rescale
-    // (src/nesterov.rs:47-55) rides on this pass: the WA gradient is complete and
-    // the density gradient is produced here, so no extra launch per step.
-    const bool do_rescale = rescale && st->iteration == 0;   // grid-uniform
-    double sa = 0.0, sb = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
-        const float sx = cw[i], sy = ch[i];
-        const float nx = x[i] + offx[i], ny = y[i] + offy[i], r = ratio[i];
+    // the field gathered over cell i's bins (src/eforce.rs)
+    auto force = [&](int i, float nx, float ny, float sx, float sy, float r) {
         long long xl = to_isize0((nx - 0.0f) * inv_bw);
         if (xl < 0) xl = 0;
         long long xh = to_isize0((nx + sx - 0.0f) * inv_bw) + 1;
@@ -642,13 +636,21 @@ __global__ void __launch_bounds__(kThreads) k_force(
         }
         gx_out[i] = -gx * r;
         gy_out[i] = -gy * r;
-    }
-    if (do_rescale) {
-        // a loop of its own: FP64 work predicated inside the loop above would
-        // occupy the FP64 pipe on every step, not only at iteration 0
+    };
+    // Inside the step graph (rescale = 1) the iteration-0 density-weight rescale
+    // (src/nesterov.rs:47-55) rides on this pass: the WA gradient is complete and
+    // the density gradient is produced here, so no extra launch per step.  That
+    // pass runs in cell order, so its FP64 sums have a fixed grouping; every
+    // other pass takes the cells in the scatter order, where a block's cells
+    // share a tile and so share field lines (the outputs are per cell: the same
+    // in any order).
+    if (rescale && st->iteration == 0) {   // grid-uniform
+        double sa = 0.0, sb = 0.0;
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
+            const float2 q = xy[i];
+            force(i, q.x + offx[i], q.y + offy[i], cw[i], ch[i], ratio[i]);
             sa += (double)fabsf(wlgx[i]) + (double)fabsf(wlgy[i]);
-            sb += (double)fabsf(gx_out[i]) + (double)fabsf(gy_out[i]);   // written by this thread above
+            sb += (double)fabsf(gx_out[i]) + (double)fabsf(gy_out[i]);   // written by this thread
         }
         double vals[2];
         vals[0] = block_sum(sa, shr);
@@ -663,6 +665,13 @@ __global__ void __launch_bounds__(kThreads) k_force(
                 st->ctr[CTR_ABS] = 0;
             }
         }
+        return;
+    }
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < NM; p += gridDim.x * blockDim.x) {
+        const int i = perm[p];
+        const float2 q = xy[i];
+        const float4 o = soff[p];   // offx, offy, cw, ch of cell i
+        force(i, q.x + o.x, q.y + o.y, o.z, o.w, sratio[p]);
     }
 }
 
@@ -1054,8 +1063,8 @@ void launch_initial_density(Ctx &c, const float *, const float *, const float *,
 
 void launch_force(Ctx &c, int rescale) {
     k_force<<<grid_for(c.NM, 152 * 16), kThreads, 0, c.stream>>>(
-        c.NM, c.x, c.y, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw,
-        c.inv_bh, c.fx, c.fy, c.dgx, c.dgy, rescale, c.wlgx, c.wlgy, c.partials, c.st);
+        c.NM, c.perm, c.xy, c.soff, c.sratio, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w, c.bin_h,
+        c.inv_bw, c.inv_bh, c.fx, c.fy, c.dgx, c.dgy, rescale, c.wlgx, c.wlgy, c.partials, c.st);
 }
 
 void launch_energy(Ctx &c) {
