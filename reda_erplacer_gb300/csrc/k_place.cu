@@ -236,9 +236,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_wa(WaArgs a, WaClasses cl, floa
     if (st->done) return;
     const float gamma = gamma_arg > 0.f ? gamma_arg : st->gamma;
     a.inv_gamma = 1.0f / gamma;                        // src/hpwl.rs:166
+    // the large-degree classes (longest blocks) take the first block indices, so
+    // they are dispatched first and the short blocks fill in behind them
+    const int vb = (int)gridDim.x - 1 - (int)blockIdx.x;
     int k = 0;
-    while (k + 1 < kNumClasses && (int)blockIdx.x >= cl.block0[k + 1]) ++k;
-    const int cb = blockIdx.x - cl.block0[k], cg = cl.block0[k + 1] - cl.block0[k];
+    while (k + 1 < kNumClasses && vb >= cl.block0[k + 1]) ++k;
+    const int cb = vb - cl.block0[k], cg = cl.block0[k + 1] - cl.block0[k];
     float hp;
 #define ERP_WA_EXACT(K, D) \
     case K: hp = wa_exact<D>(a, cl.begin[K], cl.count[K], cl.slot0[K], cl.general[K], cb, cg); break;
