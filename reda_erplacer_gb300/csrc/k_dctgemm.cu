@@ -129,9 +129,10 @@ template <int KIND, int BN>
 struct GemmCfg {
     static constexpr int kABytes = kTile * 128, kBBytes = BN * 128;
     static constexpr int kStageBytes = (KIND == 0 ? 1 : 2) * (kABytes + kBBytes);
-    // as many stages as fit (about 190 KB in flight per SM; TF32 128 x 64 tiles
-    // run two CTAs per SM)
-    static constexpr int kStages = KIND == 0 ? (BN == 128 ? 6 : 4) : (BN == 128 ? 3 : 4);
+    // TF32: 3-4 stages (96-99 KB), so two CTAs share an SM and the 128 x 128
+    // launches of a 2048^2 solve run in one wave (6 stages: 311 -> 3 stages: 247 us
+    // per solve, same bits); BF16 hi/lo stages are twice as large (one CTA per SM)
+    static constexpr int kStages = KIND == 0 ? (BN == 128 ? 3 : 4) : (BN == 128 ? 3 : 4);
     static constexpr int kBK = KIND == 0 ? 32 : 64;             // K elements per stage (128 bytes)
     static constexpr size_t kSmem = (size_t)kStages * kStageBytes + 1024;
 };
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm_nt(const __grid_constant__ Gemm
     const int tile_m = blockIdx.y * kTile, tile_n = blockIdx.x * BN;
     const int KT = K / Cfg::kBK;
 
-    if (warp == 0) {   // 128 accumulator columns; one CTA per SM (shared memory), so no contention
+    if (warp == 0) {   // BN accumulator columns; at most two CTAs per SM, so at most 256 of the 512 columns
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
                      "r"(BN)
                      : "memory");

@@ -146,6 +146,30 @@ def test_step_matches_stage_sequence(R, O):
     assert np.array_equal(xa, xb) and np.array_equal(ya, yb)
 
 
+@pytest.mark.parametrize("steps", [16, 40])
+def test_density_map_in_the_scatter_order(R, O, steps):
+    """The scatter takes the cells in a spatial order recomputed every 16 steps;
+    after `steps` steps (the order recomputed, then the cells moved on) the int64
+    map of the current positions is still bit-exact against the oracle's."""
+    d = small_synth(20000, seed=31, macros=2, io=200)
+    g = R.Placement(d, (256, 128), 1.0, start_mode=1)
+    o = O.Oracle(d, 256, 128, target_density=1.0, start_mode=O.START_DB, density_mode=O.DENSITY_FIXED,
+                 reduce_fp64=1)
+    try:
+        for _ in range(steps):
+            g.step(stats=False)
+        x, y = g.positions()
+        o.set_positions(x, y)
+        _, ovo = o.compute_potential(0)
+        _, ovg = g.compute_potential(0)
+        assert np.array_equal(g.array("DENSITY_I64"), o.get("density_i64"))
+        assert abs(ovg - ovo) <= 1e-6 * max(abs(ovo), 1e-12)
+        assert rel_l2(g.array("FIELD_X"), o.get("field_x")) <= TOL
+    finally:
+        g.close()
+        o.close()
+
+
 def test_step_host_matches_step(R):
     d = small_synth(2000, seed=22)
     a = R.Placement(d, (64, 64), 1.0)
