@@ -242,6 +242,7 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     c.device = prm.device;
     CK(spectral_prepare());
     CK(place_prepare());
+    CK(place_occupancy());
     const int N = d->num_nodes, NM = d->num_movable, P = d->num_pins, E = d->num_nets;
     c.N = N; c.NM = NM; c.P = P; c.E = E; c.NS = P;
     c.m = prm.num_bins_x; c.n = prm.num_bins_y;

@@ -1064,8 +1064,13 @@ void launch_initial_density(Ctx &c, const float *, const float *, const float *,
         mn, c.dmap, ldexpf(1.0f, -c.shift0), c.target_density, c.initial);
 }
 
+// Blocks of the streaming kernels that fit on the GPU at once: their grids stop
+// there (grid-stride loops), so no partial last wave runs alone.
+static int g_res_force = 0, g_res_grad = 0, g_res_update = 0;
+static int fit(int need, int resident) { return resident > 0 && need > resident ? resident : need; }
+
 void launch_force(Ctx &c, int rescale) {
-    k_force<<<grid_for(c.NM, 152 * 16), kThreads, 0, c.stream>>>(
+    k_force<<<fit(grid_for(c.NM, 152 * 16), g_res_force), kThreads, 0, c.stream>>>(
         c.NM, c.perm, c.xy, c.soff, c.sratio, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w, c.bin_h,
         c.inv_bw, c.inv_bh, c.fx, c.fy, c.dgx, c.dgy, rescale, c.wlgx, c.wlgy, c.partials, c.st);
 }
@@ -1083,11 +1088,25 @@ void launch_nesterov(Ctx &c, int iter_arg) {
                                                    c.partials, c.st);
     }
     const int g4 = grid_for((c.NM + 3) / 4);
-    k_nesterov_grad<<<g4, kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx, c.dgy, c.w,
+    k_nesterov_grad<<<fit(g4, g_res_grad), kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx, c.dgy, c.w,
                                                   c.h, c.npins, c.x, c.y, c.prev_x, c.prev_y,
                                                   c.prev_gx, c.prev_gy, c.partials, c.st);
-    k_nesterov_update<<<g4, kThreads, 0, c.stream>>>(c.NM, c.w, c.h, c.die_w, c.die_h, c.x, c.y,
+    k_nesterov_update<<<fit(g4, g_res_update), kThreads, 0, c.stream>>>(c.NM, c.w, c.h, c.die_w, c.die_h, c.x, c.y,
                                                     c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.xy, c.st);
+}
+
+cudaError_t place_occupancy() {
+    int dev = 0, sms = 0, a = 0, b = 0, d = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_force, kThreads, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_nesterov_grad, kThreads, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_nesterov_update, kThreads, 0);
+    if (e != cudaSuccess) return e;
+    g_res_force = a * sms;
+    g_res_grad = b * sms;
+    g_res_update = d * sms;
+    return cudaSuccess;
 }
 
 void launch_pack_xy(Ctx &c) {
