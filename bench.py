@@ -143,6 +143,27 @@ def barrier(world):
         dist.barrier()
 
 
+def allreduce_sum(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def gather_items(items, world):
+    """Concatenate every rank's list (rank order); the only cross-rank step of
+    the sharded batch and serving sections besides the max of their times."""
+    if world == 1:
+        return list(items)
+    import torch.distributed as dist
+    out = [None] * world
+    dist.all_gather_object(out, list(items))
+    return [x for part in out for x in part]
+
+
 def make_workload(name):
     import reda_erplacer_gb300 as R
     if name == "large":
@@ -170,17 +191,23 @@ def cpu_sample(d, cfg, iters, literal):
     return iters / dt, dt
 
 
-def batch_section(args, device):
+def batch_section(args, device, world=1, rank=0):
     """Batched workload: 64 instances (cells log-uniform 2k-200k, nets 1.05x,
     macros 0-16, bins = pow2 nearest sqrt(cells)/2 in 64..1024), each to 600
     iterations or overflow <= 0.10.  Jobs/hour of the batched graph (all
     instances in one CUDA graph) against running the same jobs one at a time
-    through erp_run; both include context creation."""
+    through erp_run; both include context creation.  With several ranks the
+    instances are sharded over the GPUs (host-side dispatch, no collective) and
+    each time is the maximum over the ranks."""
     import torch
     import reda_erplacer_gb300 as R
-    mix = R.workload_batch(count=args.batch_count)
+    from reda_erplacer_gb300.dispatch import job_cost, rank_jobs
+    full = R.workload_batch(count=args.batch_count)
+    mine = rank_jobs([job_cost(d.num_movable, args.batch_iters) for d, _ in full], world, rank)
+    mix = [full[i] for i in mine]
     designs = [d for d, _ in mix]
     bins = [b for _, b in mix]
+    barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     bt = R.Batch(designs, bins, 1.0, start_mode=1, device=device)
@@ -213,8 +240,22 @@ def batch_section(args, device):
     torch.cuda.synchronize()
     t_mixed = time.perf_counter() - t0
     bm.close()
+    # across ranks: times are the slowest rank's, counts and lists are gathered
+    t_batch, t_seq, t_mixed = (allreduce_max(t, world) for t in (t_batch, t_seq, t_mixed))
+    t_bcreate, t_screate = allreduce_max(t_bcreate, world), allreduce_max(t_screate, world)
+    rows = sorted(gather_items([(i, int(a), int(b), int(c), la["overflow"], la["hpwl"], lm["overflow"], lm["hpwl"], q)
+                                for i, a, b, c, la, lm, q in zip(mine, its, seq_its, its_m, lasts, lasts_m, seq_lat)],
+                               world))
+    precs_all = gather_items([int(p != R.lib.PREC_FP32) for p in precs], world)
+    K = len(full)
+    its, seq_its, its_m = [r[1] for r in rows], [r[2] for r in rows], [r[3] for r in rows]
+    lasts = [{"overflow": r[4], "hpwl": r[5]} for r in rows]
+    lasts_m = [{"overflow": r[6], "hpwl": r[7]} for r in rows]
+    seq_lat = [r[8] for r in rows]
+    designs = [d for d, _ in full]
+    bins = [b for _, b in full]
     return {
-        "instances": K, "cells": [int(d.num_movable) for d in designs],
+        "instances": K, "ranks": world, "cells": [int(d.num_movable) for d in designs],
         "bins": [int(b[0]) for b in bins], "max_iterations": args.batch_iters, "stop_overflow": 0.10,
         "iterations_total": int(sum(its)), "retired_at_overflow": int(sum(1 for l in lasts if l["overflow"] <= 0.10)),
         "batched_s": t_batch, "sequential_s": t_seq,
@@ -225,7 +266,7 @@ def batch_section(args, device):
         "spectral": "FP32 FFT (batched and sequential)",
         "mixed_batched": {
             "spectral": "BF16 hi/lo x3 tensor-core contractions (bins >= 128), FP32 FFT (64^2 bins)",
-            "instances_bf16x3": int(sum(1 for p in precs if p != R.lib.PREC_FP32)),
+            "instances_bf16x3": int(sum(precs_all)),
             "batched_s": t_mixed, "jobs_per_hour": K / t_mixed * 3600.0,
             "speedup_vs_fp32_one_at_a_time": t_seq / t_mixed,
             "iterations_total": int(sum(its_m)),
@@ -415,38 +456,47 @@ class LazyJobs:
         self.ex.shutdown(wait=False, cancel_futures=True)
 
 
-def serve_section(args, device):
+def serve_section(args, device, world=1, rank=0):
     """Serving workload: an open-loop stream of jobs (cells log-uniform 5k-500k,
     each its own seed) with Poisson arrivals at 80 % of the capacity measured by
     a batched pilot run; admission under a 150 GB HBM budget, retire at overflow
     <= 0.10 or 600 iterations.  p50/p99 completion latency and jobs/hour of the
     continuous-batching server, and of the same stream served one job at a
-    time."""
+    time.  With several ranks each GPU runs its own server, the capacity is the
+    sum of the ranks' pilots and each arriving job is routed to the rank with
+    the least assigned work (host-side dispatch, no collective)."""
     import numpy as np
     import reda_erplacer_gb300 as R
+    from reda_erplacer_gb300.dispatch import job_cost, route_stream
     from reda_erplacer_gb300.serving import Server, run_stream
     specs = R.design.batch_specs(count=args.serve_jobs, seed=9000, min_cells=5000, max_cells=500000)
     pilot = [R.design.batch_job(*sp) for sp in specs[: min(32, len(specs))]]
     bt = R.Batch([d for d, _ in pilot], [b for _, b in pilot], 1.0, start_mode=1, device=device)
     t0 = time.perf_counter()
     bt.run(args.batch_iters, stop_overflow=0.10)
-    cap = len(pilot) / (time.perf_counter() - t0)
+    cap = allreduce_sum(len(pilot) / (time.perf_counter() - t0), world)
     bt.close()
     del pilot
     rate = 0.8 * cap
     rng = np.random.default_rng(17)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(specs)))
-    out = {"jobs": len(specs), "capacity_jobs_per_s": cap, "arrival_rate_jobs_per_s": rate,
+    route = route_stream([job_cost(sp[0]) for sp in specs], world)
+    mine = [i for i, r in enumerate(route) if r == rank]
+    out = {"jobs": len(specs), "ranks": world, "capacity_jobs_per_s": cap, "arrival_rate_jobs_per_s": rate,
            "hbm_budget_gb": 150.0, "max_iterations": args.batch_iters, "stop_overflow": 0.10}
     for name, max_active in (("continuous_batching", 64), ("one_at_a_time", 1)):
-        jobs = LazyJobs(specs)
+        jobs = LazyJobs([specs[i] for i in mine])
         sv = Server(max_active=max_active, hbm_budget_gb=150.0, max_iterations=args.batch_iters,
                     stop_overflow=0.10, chunk=8, device=device)
-        res = run_stream(sv, jobs, arrivals)
+        barrier(world)
+        res = run_stream(sv, jobs, arrivals[mine])
         sv.close()
         jobs.close()
+        span = allreduce_max(max(r["finish_s"] for r in res) - min(r["submit_s"] for r in res) if res else 0.0,
+                             world)
+        res = gather_items([{"latency_s": r["latency_s"], "status": r["status"],
+                             "last": {"overflow": r["last"]["overflow"]}} for r in res], world)
         lat = np.array([r["latency_s"] for r in res])
-        span = max(r["finish_s"] for r in res) - min(r["submit_s"] for r in res)
         out[name] = {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                      "jobs_per_hour": len(res) / span * 3600.0, "makespan_s": span,
                      "failed": int(sum(1 for r in res if r["status"] != 0)),
@@ -592,13 +642,13 @@ def run_ours(args):
         "time_to_overflow": tto,
     }
     if args.batch_count > 0:
-        line["batched"] = batch_section(args, local)
+        line["batched"] = batch_section(args, local, world, rank)
     if not args.no_spectral:
         line["spectral_solve"] = spectral_section(args, local)
     if not args.no_mixed:
         line["mixed_form"] = mixed_section(args, local, d, cfg, sc, tto)
     if args.serve_jobs > 0:
-        line["serving"] = serve_section(args, local)
+        line["serving"] = serve_section(args, local, world, rank)
     if rank == 0 and world == 1 and not args.no_cpu:
         v, dt = cpu_sample(d, cfg, args.cpu_iters, literal=False)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
