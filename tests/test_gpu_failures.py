@@ -1,0 +1,73 @@
+"""Failure handling on the GPU without a fault.
+
+* A non-finite position retires the context through the step's own check on the
+  device (non-finite HPWL, overflow or step length): the host reads ERP_ENAN,
+  and the context stays retired.  Every index the kernels derive from a
+  position is clamped, so NaN coordinates read and write in bounds.
+* Inside the server a job that cannot be set up (a bin grid the library
+  rejects, a non-finite coordinate) fails alone on its admission worker: its
+  result carries its status, and the other jobs of the stream finish with the
+  results they have alone.
+"""
+import numpy as np
+import pytest
+
+from designs import small_synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def R(built):
+    import reda_erplacer_gb300 as R
+    return R
+
+
+def _with_nan(d, cell):
+    import copy
+    e = copy.deepcopy(d)
+    e.x = e.x.copy()
+    e.x[cell] = np.nan
+    return e
+
+
+def test_nan_position_retires_with_enan(R):
+    d = small_synth(3000, seed=41)
+    with R.Placement(d, (64, 64), 1.0, start_mode=1) as pl:
+        pl.step()
+        x, y = pl.positions()
+        x[5] = np.nan
+        pl.set_positions(x, y)
+        with pytest.raises(R.ErpError) as e:
+            for _ in range(3):
+                pl.step()
+        assert e.value.status == R.lib.ENAN
+        assert "non-finite" in str(e.value)
+        with pytest.raises(R.ErpError) as e2:   # retired: the next step reports the same
+            pl.step()
+        assert e2.value.status == R.lib.ENAN
+    # a fresh context on the same design is unaffected
+    with R.Placement(d, (64, 64), 1.0, start_mode=1) as pl:
+        it, last = pl.run(5)
+        assert it == 5 and np.isfinite(last["hpwl"])
+
+
+def test_server_isolates_failed_jobs(R):
+    from reda_erplacer_gb300.serving import Server, run_stream
+    good = [(R.synth(c, int(1.05 * c), num_io=20, seed=950 + k), (64, 64)) for k, c in enumerate((3000, 5000, 4000))]
+    bad_bins = (good[0][0], (100, 100))                 # not a power of two: erp_create rejects it
+    nan_job = (_with_nan(good[1][0], 7), (64, 64))     # a NaN coordinate: rejected at set-up
+    jobs = [good[0], bad_bins, good[1], nan_job, good[2]]
+    sv = Server(max_active=4, hbm_budget_gb=8.0, max_iterations=60, stop_overflow=0.0, chunk=8)
+    res = run_stream(sv, jobs, np.array([0.0, 0.0, 0.0, 0.01, 0.02]))
+    sv.close()
+    by_id = {r["job_id"]: r for r in res}
+    assert len(by_id) == 5
+    assert by_id[1]["status"] == R.lib.EINVAL
+    assert by_id[3]["status"] == R.lib.EINVAL
+    for i, (d, b) in ((0, good[0]), (2, good[1]), (4, good[2])):
+        r = by_id[i]
+        assert r["status"] == 0 and r["iterations"] == 60
+        with R.Placement(d, b, 1.0, start_mode=1) as pl:
+            it, last = pl.run(60)
+        assert r["last"]["hpwl"] == last["hpwl"] and r["last"]["overflow"] == last["overflow"]
