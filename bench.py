@@ -48,7 +48,7 @@ ALG_BYTES = {
 # of one --set full capture of the kernel on this workload (cold L2, the
 # profiler's default cache control); the command and figures are in
 # profiles/k_wa_1M_cells.md.
-NCU_TRAFFIC = {("large", "wirelength"): 69.092352e6 + 13.533184e6}
+NCU_TRAFFIC = {("large", "wirelength"): 69.074176e6 + 15.063040e6}
 
 
 def measured_peak_gbs():
