@@ -212,6 +212,7 @@ def batch_section(args, device, world=1, rank=0):
     t0 = time.perf_counter()
     bt = R.Batch(designs, bins, 1.0, start_mode=1, device=device)
     t_bcreate = time.perf_counter() - t0
+    tune_chosen, tune_ms = bt.tuning()
     its, lasts = bt.run(args.batch_iters, stop_overflow=0.10)
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
@@ -264,6 +265,10 @@ def batch_section(args, device, world=1, rank=0):
         "speedup": t_seq / t_batch, "same_iterations": its == seq_its,
         "sequential_latency_p50_s": float(statistics.median(seq_lat)),
         "spectral": "FP32 FFT (batched and sequential)",
+        "scatter_autotune": {"cells_per_block": tune_chosen,
+                             "candidates_ms": {str(c): round(t, 4) for c, t in tune_ms},
+                             "note": "0 = the rule of a context run alone; timed at creation, all instances' "
+                                     "scatters together; included in batched_s"},
         "mixed_batched": {
             "spectral": "BF16 hi/lo x3 tensor-core contractions (bins >= 128), FP32 FFT (64^2 bins)",
             "instances_bf16x3": int(sum(precs_all)),

@@ -249,6 +249,16 @@ erp_ctx *erp_batch_context(erp_batch *b, int32_t i);
 int32_t erp_batch_size(const erp_batch *b);
 const char *erp_batch_last_error(const erp_batch *b);
 void erp_batch_destroy(erp_batch *b);
+/* The batch's autotuned shape of the density scatter (no counterpart in the
+ * reference).  erp_batch_create times candidate block shapes -- movable cells per
+ * scatter block, 0 meaning the rule of a context run alone -- on all instances'
+ * scatters running together, and keeps, among the candidates within 10 % of the
+ * fastest, the one with the fewest blocks.  The shape decides no bit of the
+ * results.  *chosen receives it; cells[i] / ms[i] (up to cap entries) each
+ * candidate and its time; *count the number of candidates.  The environment variable ERP_BATCH_SCATTER_CELLS
+ * fixes the shape instead (count 0). */
+erp_status erp_batch_tuning(const erp_batch *b, int32_t *chosen, int32_t *cells, float *ms, int32_t cap,
+                            int32_t *count);
 
 /* ---- serving: continuous batching of placement jobs ----
  * Jobs are submitted as they arrive and wait in a FIFO queue.  Each

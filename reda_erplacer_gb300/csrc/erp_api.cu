@@ -1058,6 +1058,8 @@ extern "C" erp_status erp_restore(erp_ctx *ctx, const void *buf, size_t bytes) {
 struct erp_batch {
     std::vector<erp_ctx *> ctx;
     cudaStream_t master = nullptr;
+    int scatter_cells = 0;                 // autotuned cells per scatter block (0: the alone rule)
+    std::vector<std::pair<int, float>> tuning;   // (candidate, ms of all instances' scatters together)
     cudaGraphExec_t graph = nullptr;
     bool graph_ready = false;
     int graph_kernels = 0;
@@ -1067,6 +1069,8 @@ struct erp_batch {
     int device = 0;
     std::string err;
 };
+
+static erp_status batch_tune_scatter(erp_batch *b);
 
 static erp_status batch_fail(erp_batch *b, erp_status s, const std::string &msg) {
     b->err = msg;
@@ -1135,12 +1139,122 @@ extern "C" erp_status erp_batch_create(const erp_design *designs, const erp_para
             g_create_err = "batch allocation failed";
         }
     }
+    if (s == ERP_OK) {
+        s = batch_tune_scatter(b);
+        if (s != ERP_OK) g_create_err = b->err;
+    }
     if (s != ERP_OK) {
         erp_batch_destroy(b);
         return s;
     }
     *out = b;
     return ERP_OK;
+}
+
+extern "C" erp_status erp_batch_tuning(const erp_batch *b, int32_t *chosen, int32_t *cells, float *ms, int32_t cap,
+                                       int32_t *count) {
+    if (!b || cap < 0 || (cap > 0 && (!cells || !ms))) return ERP_EINVAL;
+    if (chosen) *chosen = b->scatter_cells;
+    const int k = std::min<int>(cap, (int)b->tuning.size());
+    for (int i = 0; i < k; ++i) {
+        cells[i] = b->tuning[i].first;
+        ms[i] = b->tuning[i].second;
+    }
+    if (count) *count = (int32_t)b->tuning.size();
+    return ERP_OK;
+}
+
+// Autotuner of the scatter's block shape for a batch.  Run alone a context
+// spreads its cells over many small blocks; with every instance of a batch on the
+// GPU at once, fewer fuller blocks (fewer windows to clear and flush) measured
+// faster.  Each candidate is timed on a graph of all instances' scatters running
+// together; the scatter only adds into the int64 map, which is cleared again
+// afterwards, so no placement state changes, and the block shape decides no bit
+// of the map.  It runs once, at creation (a second calibration after 128
+// iterations, with the cells spread, chose the same shape on the 64-design mix
+// and only cost its time).  ERP_BATCH_SCATTER_CELLS=<n> fixes the choice instead.
+static erp_status batch_tune_scatter(erp_batch *b) {
+    const int cand[] = {0, 512, 1024, 2048};
+    if (const char *env = getenv("ERP_BATCH_SCATTER_CELLS")) {
+        const int v = atoi(env);
+        b->scatter_cells = v < 0 ? 0 : std::min(v, 2048);
+        for (auto *x : b->ctx) x->c.scatter_cells = b->scatter_cells;
+        return ERP_OK;
+    }
+    cudaEvent_t fork, e0, e1;
+    if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) return ERP_ECUDA;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    std::vector<cudaEvent_t> joins(b->ctx.size());
+    for (auto &e : joins) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    float best = 0.0f;
+    int best_c = 0;
+    erp_status rc = ERP_OK;
+    b->tuning.clear();
+    for (int c : cand) {
+        for (auto *x : b->ctx) x->c.scatter_cells = c;
+        cudaGraph_t g;
+        cudaGraphExec_t ge = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(b->master, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaEventRecord(fork, b->master);
+            for (size_t i = 0; i < b->ctx.size(); ++i) {
+                Ctx &x = b->ctx[i]->c;
+                cudaStreamWaitEvent(x.stream, fork, 0);
+                cudaMemsetAsync(x.dmap, 0, sizeof(unsigned long long) * (size_t)x.m * x.n, x.stream);
+                launch_density_scatter(x);
+                cudaEventRecord(joins[i], x.stream);
+                cudaStreamWaitEvent(b->master, joins[i], 0);
+            }
+            e = cudaStreamEndCapture(b->master, &g);
+        }
+        if (e == cudaSuccess) {
+            e = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+        }
+        float ms = 0.0f;
+        if (e == cudaSuccess) {
+            cudaGraphLaunch(ge, b->master);   // warm-up
+            cudaEventRecord(e0, b->master);
+            for (int r = 0; r < 3; ++r) cudaGraphLaunch(ge, b->master);
+            cudaEventRecord(e1, b->master);
+            e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+            cudaGraphExecDestroy(ge);
+        }
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            b->err = std::string("scatter autotune: ") + cudaGetErrorString(e);
+            rc = ERP_ECUDA;
+            break;
+        }
+        b->tuning.emplace_back(c, ms / 3.0f);
+        if (b->tuning.size() == 1 || ms < best) best = ms;
+    }
+    // The calibration runs the scatters alone, where more, smaller blocks look
+    // better than they are inside the step graph, which runs the other passes of
+    // every instance beside them (whole runs of the 64-design mix: 2048 cells per
+    // block 512k jobs/h, 1024 494k, 512 467k, the alone rule 431k).  So among the
+    // candidates within 10 % of the fastest the one with the fewest blocks wins.
+    for (const auto &t : b->tuning) {
+        const int c = t.first;
+        const bool fewer = c == 0 ? false : (best_c == 0 || c > best_c);
+        if (t.second * 3.0f <= 1.10f * best && fewer) best_c = c;
+    }
+    if (best_c == 0)
+        for (const auto &t : b->tuning)
+            if (t.second * 3.0f <= best) best_c = t.first;
+    b->scatter_cells = rc == ERP_OK ? best_c : 0;
+    for (auto *x : b->ctx) {   // the maps are cleared again: the calibration leaves no trace
+        x->c.scatter_cells = b->scatter_cells;
+        cudaMemsetAsync(x->c.dmap, 0, sizeof(unsigned long long) * (size_t)x->c.m * x->c.n, b->master);
+    }
+    if (cudaStreamSynchronize(b->master) != cudaSuccess && rc == ERP_OK) rc = ERP_ECUDA;
+    cudaEventDestroy(fork);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (auto &e : joins) cudaEventDestroy(e);
+    return rc;
 }
 
 // (Re)capture the batch graph over the instances whose active flag is set.
@@ -1425,6 +1539,9 @@ static void server_worker(erp_server *sv) {
         erp_status s = erp_create(&j->des->d, &j->prm, &j->ctx);
         if (s == ERP_OK) {
             Ctx &c = j->ctx->c;
+            // jobs that share the GPU take the batch's scatter shape: fewer, fuller
+            // blocks (the shape the batch calibration keeps on the 64-design mix)
+            if (sv->p.max_active > 1) c.scatter_cells = 2048;
             c.h_st->stop_overflow = sv->p.stop_overflow > 0 ? sv->p.stop_overflow : 0.0f;
             c.h_st->stop_iter = sv->p.max_iterations;
             c.h_st->done = 0;

@@ -102,6 +102,7 @@ struct Ctx {
     float *sratio;
     int32_t *sort_key, *sort_rank, *sort_hist, *sort_start;   // counting-sort scratch ([NM], [NM], tiles, tiles)
     int32_t sort_age;          // steps since the order was computed
+    int32_t scatter_cells;     // movable cells per scatter block; 0: the rule for a context run alone
     // host-side permutations for test hooks
     int32_t *h_slot_of_pin;    // [P]
     int32_t *h_net_of_internal;// [E]

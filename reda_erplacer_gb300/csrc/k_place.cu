@@ -1011,8 +1011,15 @@ void launch_wl_gather(Ctx &c) {
                                                            c.slot_grad, c.wlgx, c.wlgy, c.st);
 }
 
+// Blocks of the scatter.  Alone, a context spreads its cells over up to 608
+// blocks (four per SM); a batch autotunes the cells per block, since with many
+// instances on the GPU at once fewer, fuller blocks flush fewer windows (see
+// erp_batch_create).  Never more than kMaxCellsPerBlock cells per block (the
+// window's 21-bit pieces rely on it); the grid decides no bit of the map.
 void launch_density_scatter(Ctx &c) {
-    const int g = std::max(grid_for(c.NM, 152 * 4), (c.NM + kMaxCellsPerBlock - 1) / kMaxCellsPerBlock);
+    const int floor_g = (c.NM + kMaxCellsPerBlock - 1) / kMaxCellsPerBlock;
+    const int g = c.scatter_cells > 0 ? std::max((c.NM + c.scatter_cells - 1) / c.scatter_cells, std::max(floor_g, 1))
+                                      : std::max(grid_for(c.NM, 152 * 4), floor_g);
     const int nty = (c.n + kSortTile - 1) / kSortTile;
     k_density_scatter<<<g, kThreads, density_scatter_smem(), c.stream>>>(
         c.NM, c.perm, c.xy, c.soff, c.sratio, c.skey, nty, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw,

@@ -233,6 +233,14 @@ class Batch:
             raise L.ErpError(st, self.lib.erp_batch_last_error(self.h).decode())
         return [int(v) for v in it], [s.as_dict() for s in last]
 
+    def tuning(self):
+        """The autotuned scatter shape: (chosen cells per block, [(candidate, ms), ...])."""
+        ch, n = C.c_int32(), C.c_int32()
+        cells = (C.c_int32 * 8)()
+        ms = (C.c_float * 8)()
+        L.check(self.lib.erp_batch_tuning(self.h, C.byref(ch), cells, ms, 8, C.byref(n)))
+        return int(ch.value), [(int(cells[i]), float(ms[i])) for i in range(min(n.value, 8))]
+
     def positions(self, i):
         ctx = self.lib.erp_batch_context(self.h, int(i))
         N = int(self.designs[i].num_nodes)

@@ -266,6 +266,37 @@ def test_spectral_standalone_fp64_error(R, O):
     assert max(ex, ey, ep) <= 1e-5
 
 
+def test_batch_scatter_autotune(R):
+    """erp_batch_create times the scatter's block shapes on all instances at once
+    and keeps the fastest; a fixed shape (environment) gives the same results."""
+    import os
+    mix = R.workload_batch(count=6, seed=77, min_cells=2000, max_cells=30000)
+    designs, bins = [d for d, _ in mix], [b for _, b in mix]
+    bt = R.Batch(designs, bins, 1.0, start_mode=1)
+    chosen, cand = bt.tuning()
+    assert [c for c, _ in cand] == [0, 512, 1024, 2048] and all(t > 0 for _, t in cand)
+    best = min(t for _, t in cand)
+    fastest_few = max((c for c, t in cand if c > 0 and t <= 1.10 * best + 1e-6), default=None)
+    assert chosen == (fastest_few if fastest_few is not None else min(cand, key=lambda ct: ct[1])[0])
+    its, lasts = bt.run(200)
+    assert bt.tuning() == (chosen, cand)
+    xs = [bt.positions(i) for i in range(len(mix))]
+    bt.close()
+    for forced in ("0", "2048"):
+        os.environ["ERP_BATCH_SCATTER_CELLS"] = forced
+        try:
+            b2 = R.Batch(designs, bins, 1.0, start_mode=1)
+            assert b2.tuning() == (int(forced), [])
+            its2, lasts2 = b2.run(200)
+            assert its2 == its and [l["hpwl"] for l in lasts2] == [l["hpwl"] for l in lasts]
+            for i in range(len(mix)):
+                xa, ya = b2.positions(i)
+                assert np.array_equal(xa, xs[i][0]) and np.array_equal(ya, xs[i][1])
+            b2.close()
+        finally:
+            del os.environ["ERP_BATCH_SCATTER_CELLS"]
+
+
 def test_batch_matches_individual_runs(R):
     """Instances advanced together in one batched graph end bit-identical to the
     same designs run alone (each instance's kernels are the same; only their
