@@ -637,16 +637,40 @@ extern "C" erp_status erp_step(erp_ctx *ctx, erp_step_stats *stats) {
     return ERP_OK;
 }
 
+// The device address of a registered (pinned, device-mapped) host buffer, or
+// nullptr for any other memory.
+static float *mapped_host(float *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? static_cast<float *>(a.devicePointer) : nullptr;
+}
+
 extern "C" erp_status erp_step_host(erp_ctx *ctx, float *x, float *y, erp_step_stats *stats) {
     CTX_CHECK();
     if (!x || !y) return ERP_EINVAL;
-    CK(cudaMemcpyAsync(c.x, x, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
-    CK(cudaMemcpyAsync(c.y, y, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
-    launch_pack_xy(c);
+    // Registered host buffers are read and written by the device itself (one pass
+    // each way, no staging); other host memory goes through copies.
+    float *dx = mapped_host(x), *dy = mapped_host(y);
+    const bool direct = dx && dy;
+    if (direct) {
+        launch_xy_from_host(c, dx, dy);
+    } else {
+        CK(cudaMemcpyAsync(c.x, x, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+        CK(cudaMemcpyAsync(c.y, y, sizeof(float) * c.N, cudaMemcpyHostToDevice, c.stream));
+        launch_pack_xy(c);
+    }
     erp_status s = enqueue_step(c);
     if (s != ERP_OK) return s;
-    CK(cudaMemcpyAsync(x, c.x, sizeof(float) * c.N, cudaMemcpyDeviceToHost, c.stream));
-    CK(cudaMemcpyAsync(y, c.y, sizeof(float) * c.N, cudaMemcpyDeviceToHost, c.stream));
+    if (direct) {
+        launch_xy_to_host(c, dx, dy);
+    } else {
+        CK(cudaMemcpyAsync(x, c.x, sizeof(float) * c.N, cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaMemcpyAsync(y, c.y, sizeof(float) * c.N, cudaMemcpyDeviceToHost, c.stream));
+    }
+    CK(cudaGetLastError());
     s = pull_state(c);
     if (stats) *stats = c.h_st->last;
     return s;

@@ -143,6 +143,8 @@ void launch_density_scatter(Ctx &c);
 void launch_spectral(Ctx &c, bool zero_map, bool store_rho, bool want_psi);
 void launch_scatter_order(Ctx &c, cudaStream_t s);   // recompute the scatter order from the current positions
 int scatter_tiles(int m, int n);
+void launch_xy_from_host(Ctx &c, const float *hx, const float *hy);   // device-mapped host x, y -> x, y, xy
+void launch_xy_to_host(Ctx &c, float *hx, float *hy);                 // xy -> device-mapped host x, y
 cudaError_t place_occupancy();                        // resident block counts of the streaming kernels
 constexpr int kSortEvery = 16;                          // steps between scatter-order refreshes
 void launch_force(Ctx &c, int rescale);                   // rescale 1: also the iteration-0 density-weight rescale (step graph)

@@ -884,6 +884,27 @@ __global__ void k_pack_xy(int N, const float *__restrict__ x, const float *__res
         xy[i] = make_float2(x[i], y[i]);
 }
 
+// The host's coordinates read and written by the device directly (registered,
+// device-mapped host memory; over NVLink-C2C on a Grace host): one pass fills
+// x, y and the interleaved xy, one pass writes the step's result back.
+__global__ void k_xy_from_host(int N, const float *__restrict__ hx, const float *__restrict__ hy,
+                               float *__restrict__ x, float *__restrict__ y, float2 *__restrict__ xy) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        const float a = hx[i], b = hy[i];
+        x[i] = a;
+        y[i] = b;
+        xy[i] = make_float2(a, b);
+    }
+}
+
+__global__ void k_xy_to_host(int N, const float2 *__restrict__ xy, float *__restrict__ hx, float *__restrict__ hy) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        const float2 v = xy[i];
+        hx[i] = v.x;
+        hy[i] = v.y;
+    }
+}
+
 // ============================ scheduler ============================
 // Scheduler::update + should_stop (src/scheduler.rs:68-130) in FP64, plus the
 // step record, the non-finite check and the retire-at-overflow flag.
@@ -1118,6 +1139,61 @@ cudaError_t place_occupancy() {
 
 void launch_pack_xy(Ctx &c) {
     if (c.N > 0) k_pack_xy<<<grid_for(c.N), kThreads, 0, c.stream>>>(c.N, c.x, c.y, c.xy);
+}
+
+// Four cells per thread with 16-byte accesses when both host buffers allow it:
+// fewer, larger requests across the host link.
+__global__ void k_xy_from_host4(int N, const float4 *__restrict__ hx, const float4 *__restrict__ hy,
+                                float4 *__restrict__ x, float4 *__restrict__ y, float4 *__restrict__ xy) {
+    const int n4 = N >> 2;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
+        const float4 a = hx[i], b = hy[i];
+        x[i] = a;
+        y[i] = b;
+        xy[2 * i] = make_float4(a.x, b.x, a.y, b.y);
+        xy[2 * i + 1] = make_float4(a.z, b.z, a.w, b.w);
+    }
+}
+
+__global__ void k_xy_to_host4(int N, const float4 *__restrict__ xy, float4 *__restrict__ hx, float4 *__restrict__ hy) {
+    const int n4 = N >> 2;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
+        const float4 p = xy[2 * i], q = xy[2 * i + 1];
+        hx[i] = make_float4(p.x, p.z, q.x, q.z);
+        hy[i] = make_float4(p.y, p.w, q.y, q.w);
+    }
+}
+
+static bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+void launch_xy_from_host(Ctx &c, const float *hx, const float *hy) {
+    if (c.N <= 0) return;
+    const int n4 = c.N >> 2;
+    if (n4 > 0 && aligned16(hx) && aligned16(hy)) {   // device arrays are 256-byte aligned
+        k_xy_from_host4<<<grid_for(n4), kThreads, 0, c.stream>>>(c.N, reinterpret_cast<const float4 *>(hx),
+                                                                 reinterpret_cast<const float4 *>(hy),
+                                                                 reinterpret_cast<float4 *>(c.x),
+                                                                 reinterpret_cast<float4 *>(c.y),
+                                                                 reinterpret_cast<float4 *>(c.xy));
+        const int t = n4 << 2;   // the tail
+        if (t < c.N) k_xy_from_host<<<1, 32, 0, c.stream>>>(c.N - t, hx + t, hy + t, c.x + t, c.y + t, c.xy + t);
+        return;
+    }
+    k_xy_from_host<<<grid_for(c.N), kThreads, 0, c.stream>>>(c.N, hx, hy, c.x, c.y, c.xy);
+}
+
+void launch_xy_to_host(Ctx &c, float *hx, float *hy) {
+    if (c.N <= 0) return;
+    const int n4 = c.N >> 2;
+    if (n4 > 0 && aligned16(hx) && aligned16(hy)) {
+        k_xy_to_host4<<<grid_for(n4), kThreads, 0, c.stream>>>(c.N, reinterpret_cast<const float4 *>(c.xy),
+                                                               reinterpret_cast<float4 *>(hx),
+                                                               reinterpret_cast<float4 *>(hy));
+        const int t = n4 << 2;
+        if (t < c.N) k_xy_to_host<<<1, 32, 0, c.stream>>>(c.N - t, c.xy + t, hx + t, hy + t);
+        return;
+    }
+    k_xy_to_host<<<grid_for(c.N), kThreads, 0, c.stream>>>(c.N, c.xy, hx, hy);
 }
 
 void launch_scheduler(Ctx &c, int use_args, float hpwl, float overflow) {

@@ -182,6 +182,24 @@ def test_step_host_matches_step(R):
     assert np.array_equal(xa, x) and np.array_equal(ya, y)
 
 
+def test_step_host_pinned_buffers(R):
+    """Registered (pinned) host buffers are read and written by the device
+    directly; the positions are those of the device-resident step."""
+    torch = pytest.importorskip("torch")
+    d = small_synth(2000, seed=23)
+    a = R.Placement(d, (64, 64), 1.0)
+    b = R.Placement(d, (64, 64), 1.0)
+    x0, y0 = b.positions()
+    xp, yp = torch.from_numpy(x0.copy()).pin_memory(), torch.from_numpy(y0.copy()).pin_memory()
+    x, y = xp.numpy(), yp.numpy()
+    for _ in range(5):
+        a.step()
+        st = b.step_host(x, y)
+    xa, ya = a.positions()
+    assert np.array_equal(xa, x) and np.array_equal(ya, y)
+    assert st["hpwl"] == a.last_stats["hpwl"]
+
+
 @pytest.mark.parametrize("iters", [60, 100])
 def test_end_to_end_small(R, O, iters):
     """Whole loop on the 20k-cell workload from its jittered start: after the same
