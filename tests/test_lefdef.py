@@ -173,7 +173,7 @@ def test_round_trip_of_the_hand_written_design(LD, tmp_path):
     assert (r.n_2nets, r.num_movable) == (d.n_2nets, d.num_movable)
 
 
-def test_config_small_workload_through_lefdef(R, LD, tmp_path):
+def test_small_workload_through_lefdef(R, LD, tmp_path):
     """20,000 cells / 21,000 nets / 400 IO pins, written as LEF/DEF and read back."""
     d, cfg = R.workload_small()
     lef, de = str(tmp_path / "s.lef"), str(tmp_path / "s.def")
