@@ -138,3 +138,26 @@ def test_cli_matches_python_api(R, LD, small_files, tmp_path):
         h, w = snap.shape[:2]
         assert f.read(len(b"P6\n%d %d\n255\n" % (w, h))) == b"P6\n%d %d\n255\n" % (w, h)
         assert np.array_equal(np.frombuffer(f.read(), np.uint8).reshape(h, w, 3), snap)
+
+
+def test_cli_precision_and_early_stop(R, LD, small_files, tmp_path):
+    """--precision tf32 (tensor-core solve), --stop-overflow (retire early) and
+    --start db (keep the DEF coordinates) through the command-line driver."""
+    from reda_erplacer_gb300 import build
+    lef, de, cfg = small_files
+    out = str(tmp_path / "placed.def")
+    r = subprocess.run([build.CLI, "-l", lef, "-d", de, "--iterations", "450", "--bins", "256x256",
+                        "--target-density", "1.0", "--precision", "tf32", "--stop-overflow", "0.5",
+                        "--start", "db", "--out", out, "--images", str(tmp_path)],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    line = next(ln for ln in r.stdout.splitlines() if ln.startswith("[INFO] Placement took"))
+    ran = int(line.split(":")[1].split("iterations")[0])
+    over = float(line.rsplit("overflow", 1)[1])
+    assert 0 < ran < 450 and over <= 0.5
+    p = LD.read_db(lef, out)
+    assert np.isfinite(p.x).all() and np.isfinite(p.y).all()
+    # an unsupported precision for the grid is reported, not run
+    r = subprocess.run([build.CLI, "-l", lef, "-d", de, "--bins", "64x64", "--precision", "bf16x3"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 1 and "error" in r.stderr
