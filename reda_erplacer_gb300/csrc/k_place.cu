@@ -11,6 +11,8 @@
 
 #include <algorithm>
 
+#include <atomic>
+
 #include "erp_internal.cuh"
 #include "reduce.cuh"
 
@@ -1094,8 +1096,13 @@ void launch_initial_density(Ctx &c, const float *, const float *, const float *,
 
 // Blocks of the streaming kernels that fit on the GPU at once: their grids stop
 // there (grid-stride loops), so no partial last wave runs alone.
-static int g_res_force = 0, g_res_grad = 0, g_res_update = 0;
-static int fit(int need, int resident) { return resident > 0 && need > resident ? resident : need; }
+// (written by every context set-up, possibly on several host threads at once:
+// atomics, though every writer stores the same counts)
+static std::atomic<int> g_res_force{0}, g_res_grad{0}, g_res_update{0};
+static int fit(int need, const std::atomic<int> &resident_a) {
+    const int resident = resident_a.load(std::memory_order_relaxed);
+    return resident > 0 && need > resident ? resident : need;
+}
 
 void launch_force(Ctx &c, int rescale) {
     k_force<<<fit(grid_for(c.NM, 152 * 16), g_res_force), kThreads, 0, c.stream>>>(
@@ -1131,9 +1138,9 @@ cudaError_t place_occupancy() {
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_nesterov_grad, kThreads, 0);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_nesterov_update, kThreads, 0);
     if (e != cudaSuccess) return e;
-    g_res_force = a * sms;
-    g_res_grad = b * sms;
-    g_res_update = d * sms;
+    g_res_force.store(a * sms, std::memory_order_relaxed);
+    g_res_grad.store(b * sms, std::memory_order_relaxed);
+    g_res_update.store(d * sms, std::memory_order_relaxed);
     return cudaSuccess;
 }
 
