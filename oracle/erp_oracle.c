@@ -666,17 +666,18 @@ void erpo_scheduler_update(erpo_state *s, float hpwl, float overflow) {
     float lower = 0.95f, upper = 1.05f;
     float delta = s->hpwl_cur - s->hpwl_prev;
     if (s->p.reduce_fp64) {
+        /* the FP64 form: b^e of the constant bases as exp(e * ln b) */
         double power;
         if (delta < 0.0f) {
-            power = pow(0.9999, (double)s->iteration);
+            power = exp((double)s->iteration * log(0.9999));
             if (power < 0.98) power = 0.98;
         } else {
-            power = pow(1.05, -(double)delta / (double)ref);
+            power = exp(-(double)delta / (double)ref * log(1.05));
             power = power < 0.95 ? 0.95 : (power > 1.05 ? 1.05 : power);
         }
         s->dw = (float)((double)s->dw * (1.05 * power));
         double ovf = (double)s->ovf_cur;
-        double coef = pow(10.0, (ovf - 0.1) * 20.0 / 9.0 - 1.0);
+        double coef = exp(((ovf - 0.1) * 20.0 / 9.0 - 1.0) * log(10.0));
         coef = coef < 0.05 ? 0.05 : (coef > 10.0 ? 10.0 : coef);
         s->gamma = (float)((double)s->base_gamma * coef);
         return;

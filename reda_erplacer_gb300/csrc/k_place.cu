@@ -10,6 +10,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <cmath>
 
 #include <atomic>
 
@@ -908,32 +909,38 @@ __global__ void k_xy_to_host(int N, const float2 *__restrict__ xy, float *__rest
 }
 
 // ============================ scheduler ============================
+struct SchedLogs {
+    double ln_shrink, ln_grow, ln_ten;   // ln 0.9999, ln 1.05, ln 10
+};
+
 // Scheduler::update + should_stop (src/scheduler.rs:68-130) in FP64, plus the
 // step record, the non-finite check and the retire-at-overflow flag.
-__global__ void k_scheduler(int use_args, float hpwl_arg, float ovf_arg, DevState *st) {
+__global__ void k_scheduler(int use_args, float hpwl_arg, float ovf_arg, SchedLogs lg, DevState *st) {
     if (blockIdx.x != 0) return;
     if (st->done) return;   // warp-uniform
     const float hpwl = use_args ? hpwl_arg : st->hpwl_f;
     const float ovf = use_args ? ovf_arg : st->overflow_f;
     // The density-weight power (lane 0) and the gamma coefficient (lane 1) are
-    // independent FP64 powers: one convergent pow call evaluates both, with the
-    // same arguments as two calls in sequence and so the same results.
+    // independent FP64 powers of constant bases, b^e = exp(e ln b) with ln b
+    // computed on the host: one convergent exp call evaluates both.  (FP64 runs
+    // at a small fraction of the FP32 rate here; pow's own logarithm was most of
+    // this one-warp kernel's time.)
     const int lane = threadIdx.x & 31;
     const int it1 = st->iteration + 1;
     const float ref0 = st->hpwl_init_set ? st->hpwl_init : hpwl;
     const float delta0 = hpwl - st->hpwl_cur;   // hpwl_cur - hpwl_prev after the update below
-    double base, ex;
+    double lnb, ex;
     if (lane == 1) {
-        base = 10.0;
+        lnb = lg.ln_ten;
         ex = ((double)ovf - 0.1) * 20.0 / 9.0 - 1.0;
     } else if (delta0 < 0.0f) {
-        base = 0.9999;
+        lnb = lg.ln_shrink;
         ex = (double)it1;
     } else {
-        base = 1.05;
+        lnb = lg.ln_grow;
         ex = -(double)delta0 / (double)ref0;
     }
-    double pw = pow(base, ex);
+    double pw = exp(ex * lnb);
     if (lane == 1) pw = pw < 0.05 ? 0.05 : (pw > 10.0 ? 10.0 : pw);
     else if (delta0 < 0.0f) pw = pw < 0.98 ? 0.98 : pw;
     else pw = pw < 0.95 ? 0.95 : (pw > 1.05 ? 1.05 : pw);
@@ -1204,7 +1211,10 @@ void launch_xy_to_host(Ctx &c, float *hx, float *hy) {
 }
 
 void launch_scheduler(Ctx &c, int use_args, float hpwl, float overflow) {
-    k_scheduler<<<1, 32, 0, c.stream>>>(use_args, hpwl, overflow, c.st);
+    // update_density_weight's bases 0.9999 and 1.05, update_gamma's 10
+    // (src/scheduler.rs:92-130)
+    static const SchedLogs lg = {std::log(0.9999), std::log(1.05), std::log(10.0)};
+    k_scheduler<<<1, 32, 0, c.stream>>>(use_args, hpwl, overflow, lg, c.st);
 }
 
 }  // namespace erp
