@@ -226,8 +226,8 @@ __device__ __forceinline__ float wa_exact(const WaArgs &a, int net_begin, int ne
 }
 
 // All degree classes in one launch: blocks [cls_block[k], cls_block[k+1]) serve
-// class k.  The block partials of the HPWL total are summed in FP64 by the last
-// block to finish (fixed order, src/hpwl.rs:341-342).
+// class k.  The block partials of the HPWL total are summed in double-float by
+// the last block to finish (fixed order, src/hpwl.rs:341-342).
 struct WaClasses {
     int begin[kNumClasses], count[kNumClasses], general[kNumClasses], slot0[kNumClasses];
     int block0[kNumClasses + 1];
@@ -262,8 +262,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wa(WaArgs a, WaClasses cl, floa
     default: hp = wa_class<32, 4>(a, cl.begin[10], cl.count[10], cl.general[10], cb, cg); break;
     }
 #undef ERP_WA_EXACT
-    const double b = block_sum((double)hp, shr);
-    double vals[1] = {b};
+    const Df vals[1] = {block_sum(hp, shr)};
     if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_HPWL], gridDim.x)) {
         const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
         if (threadIdx.x == 0) {
@@ -282,7 +281,9 @@ __global__ void k_wl_zero(DevState *st) {
 }
 
 // compute_gradients (src/hpwl.rs:113-135): instance gradient = sum of its pin
-// gradients in macro_2_pins order; movable instances only.
+// gradients in macro_2_pins order; movable instances only.  The slot indices of
+// up to four pins are loaded, then their gradients, then summed in list order:
+// two memory round trips per four pins instead of two per pin.
 __global__ void __launch_bounds__(kThreads) k_wl_gather(int NM, const int32_t *__restrict__ ptr,
                                                         const int32_t *__restrict__ slots,
                                                         const float2 *__restrict__ g,
@@ -291,10 +292,20 @@ __global__ void __launch_bounds__(kThreads) k_wl_gather(int NM, const int32_t *_
     if (st->done) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
         float sx = 0.0f, sy = 0.0f;
-        for (int k = ptr[i], e = ptr[i + 1]; k < e; ++k) {
-            const float2 v = g[slots[k]];
-            sx += v.x;
-            sy += v.y;
+        const int e = ptr[i + 1];
+        for (int k0 = ptr[i]; k0 < e; k0 += 4) {
+            int sl[4];
+            float2 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) sl[u] = k0 + u < e ? slots[k0 + u] : -1;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = sl[u] >= 0 ? g[sl[u]] : make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (k0 + u < e) {
+                    sx += v[u].x;
+                    sy += v[u].y;
+                }
         }
         gx[i] = sx;
         gy[i] = sy;
@@ -646,19 +657,19 @@ __global__ void __launch_bounds__(kThreads) k_force(
     // Inside the step graph (rescale = 1) the iteration-0 density-weight rescale
     // (src/nesterov.rs:47-55) rides on this pass: the WA gradient is complete and
     // the density gradient is produced here, so no extra launch per step.  That
-    // pass runs in cell order, so its FP64 sums have a fixed grouping; every
+    // pass runs in cell order, so its sums have a fixed grouping; every
     // other pass takes the cells in the scatter order, where a block's cells
     // share a tile and so share field lines (the outputs are per cell: the same
     // in any order).
     if (rescale && st->iteration == 0) {   // grid-uniform
-        double sa = 0.0, sb = 0.0;
+        Df sa = df_zero(), sb = df_zero();
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
             const float2 q = xy[i];
             force(i, q.x + offx[i], q.y + offy[i], cw[i], ch[i], ratio[i]);
-            sa += (double)fabsf(wlgx[i]) + (double)fabsf(wlgy[i]);
-            sb += (double)fabsf(gx_out[i]) + (double)fabsf(gy_out[i]);   // written by this thread
+            sa = df_add(df_add(sa, fabsf(wlgx[i])), fabsf(wlgy[i]));
+            sb = df_add(df_add(sb, fabsf(gx_out[i])), fabsf(gy_out[i]));   // written by this thread
         }
-        double vals[2];
+        Df vals[2];
         vals[0] = block_sum(sa, shr);
         vals[1] = block_sum(sb, shr);
         if (arrive_last(partials, blockIdx.x, 2, vals, &st->ctr[CTR_ABS], gridDim.x)) {
@@ -681,15 +692,14 @@ __global__ void __launch_bounds__(kThreads) k_force(
     }
 }
 
-// energy = sum psi * rho (src/epotential.rs:344-346), FP64
+// energy = sum psi * rho (src/epotential.rs:344-346), double-float sums
 __global__ void k_energy(size_t mn, const float *__restrict__ psi, const float *__restrict__ rho,
                          double *__restrict__ partials, DevState *st) {
     __shared__ double shr[kThreads / 32];
-    double v = 0.0;
+    Df v = df_zero();
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < mn; k += (size_t)gridDim.x * blockDim.x)
-        v += (double)(psi[k] * rho[k]);
-    const double b = block_sum(v, shr);
-    double vals[1] = {b};
+        v = df_add(v, psi[k] * rho[k]);
+    const Df vals[1] = {block_sum(v, shr)};
     if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_ENERGY], gridDim.x)) {
         const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
         if (threadIdx.x == 0) {
@@ -712,12 +722,12 @@ __global__ void __launch_bounds__(kThreads) k_dw_rescale(int NM, int iter_arg,
     if (st->done) return;
     const int it = iter_arg >= 0 ? iter_arg : st->iteration;
     if (it != 0) return;
-    double a = 0.0, b = 0.0;
+    Df a = df_zero(), b = df_zero();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
-        a += (double)fabsf(wlgx[i]) + (double)fabsf(wlgy[i]);
-        b += (double)fabsf(dgx[i]) + (double)fabsf(dgy[i]);
+        a = df_add(df_add(a, fabsf(wlgx[i])), fabsf(wlgy[i]));
+        b = df_add(df_add(b, fabsf(dgx[i])), fabsf(dgy[i]));
     }
-    double vals[2];
+    Df vals[2];
     vals[0] = block_sum(a, shr);
     vals[1] = block_sum(b, shr);
     if (arrive_last(partials, blockIdx.x, 2, vals, &st->ctr[CTR_ABS], gridDim.x)) {
@@ -741,7 +751,7 @@ __global__ void __launch_bounds__(kThreads) k_dw_rescale(int NM, int iter_arg,
 // Both Nesterov kernels move four cells per thread with 128-bit loads and
 // stores (the per-cell arrays are 256-byte aligned; a scalar tail covers
 // NM % 4).  Each thread's Lipschitz partial over its four cells is FP32 (the
-// products are FP32 in the reference) and the block sums are FP64.
+// products are FP32 in the reference) and the block sums are double-float.
 struct Cell4 {
     float v[4];
 };
@@ -806,9 +816,9 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_grad(
         pgx[i] = gx;
         pgy[i] = gy;
     }
-    double vals[2];
-    vals[0] = block_sum((double)numf, shr);
-    vals[1] = block_sum((double)denf, shr);
+    Df vals[2];
+    vals[0] = block_sum(numf, shr);
+    vals[1] = block_sum(denf, shr);
     if (arrive_last(partials, blockIdx.x, 2, vals, &st->ctr[CTR_LIP], gridDim.x)) {
         const double tn = sum_partials(partials, gridDim.x, 2, 0, shr);
         const double td = sum_partials(partials, gridDim.x, 2, 1, shr);

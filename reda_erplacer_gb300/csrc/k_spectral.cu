@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(kThreads) k_rows_dct(
     __shared__ double shr[kThreads / 32];
     for (int k = threadIdx.x; k < (n >> 1); k += blockDim.x) tw[k] = tw_g[k];
     const int row0 = blockIdx.x * 2 * PAIRS;
-    double ovf = 0.0;
+    Df ovf = df_zero();
     for (int idx = threadIdx.x; idx < PAIRS * n; idx += blockDim.x) {
         const int p = idx >> logn, i = idx & (n - 1);
         float v[2];
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(kThreads) k_rows_dct(
                 // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
                 const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q), fixed_inv), initial[k]);
                 const float o = __fsub_rn(d, coef);
-                ovf += (double)(o > 0.0f ? o : 0.0f);      // src/epotential.rs:274-276
+                ovf = df_add(ovf, o > 0.0f ? o : 0.0f);    // src/epotential.rs:274-276
                 v[h] = __fmul_rn(d, inv_area);               // src/epotential.rs:284-285
                 if (rho_out) rho_out[k] = v[h];
             }
@@ -117,8 +117,7 @@ __global__ void __launch_bounds__(kThreads) k_rows_dct(
         t1[(size_t)(r + 1) * n + k] = 0.5f * (e.x * dy + e.y * dx);
     }
     if (!rho_in && partials) {
-        const double b = block_sum(ovf, shr);
-        double vals[1] = {b};
+        const Df vals[1] = {block_sum(ovf, shr)};
         if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_OVF], gridDim.x)) {
             const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
             if (threadIdx.x == 0) {
@@ -505,7 +504,7 @@ __global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
     }
     __syncwarp();
     const AxisTables tb = load_tables<NW, H>(sm, tw_n, ek_n);
-    double ovf = 0.0;
+    Df ovf = df_zero();
     if (from_map) {
         if (!mbar_wait(&bar[warp], 0)) {
             if (lane == 0 && st) {
@@ -516,17 +515,17 @@ __global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
         }
         const unsigned long long *q_s = reinterpret_cast<const unsigned long long *>(wbase);
         float v[2 * E];
-        double ov4[4] = {0.0, 0.0, 0.0, 0.0};   // four independent FP64 chains
+        Df ov4[4] = {df_zero(), df_zero(), df_zero(), df_zero()};   // four independent chains
 #pragma unroll
         for (int t = 0; t < 2 * E; ++t) {
             const int i = lane + 32 * t;
             // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
             const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q_s[i]), fixed_inv), ini_s[i]);
             const float o = __fsub_rn(d, coef);
-            ov4[t & 3] += (double)(o > 0.0f ? o : 0.0f);    // src/epotential.rs:274-276
+            ov4[t & 3] = df_add(ov4[t & 3], o > 0.0f ? o : 0.0f);   // src/epotential.rs:274-276
             v[t] = __fmul_rn(d, inv_area);                    // src/epotential.rs:284-285
         }
-        ovf = (ov4[0] + ov4[1]) + (ov4[2] + ov4[3]);
+        ovf = df_add(df_add(ov4[0], ov4[1]), df_add(ov4[2], ov4[3]));
         if (zero_map) {
             ulonglong2 *zr = reinterpret_cast<ulonglong2 *>(dmap + (size_t)row * N);
 #pragma unroll
@@ -550,8 +549,7 @@ __global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
     float *out = t1 + (size_t)row * N;
     warp_dct2_real<E>(xm, zb, tb.twh, tb.tw, tb.ek, lane, [&](int k, float y) { out[k] = y; });
     if (from_map && partials) {
-        const double b = block_sum(ovf, shr);
-        double vals[1] = {b};
+        const Df vals[1] = {block_sum(ovf, shr)};
         if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_OVF], gridDim.x)) {
             const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
             if (threadIdx.x == 0) {
@@ -839,7 +837,7 @@ __global__ void __launch_bounds__(G * kQ * 32) k_rows_dct_g(
     }
     const AxisTables tb = load_tables<G * kQ, H>(sm, tw_n, ek_n);
     __syncthreads();   // tables; the group's barrier initialisation
-    double ovf = 0.0;
+    Df ovf = df_zero();
     float v[PT];
     if (from_map) {
         if (!mbar_wait(&bar[grp], 0)) {
@@ -850,17 +848,17 @@ __global__ void __launch_bounds__(G * kQ * 32) k_rows_dct_g(
             mbar_wait(&bar[grp], 0);   // the copy must land before the area is reused
         }
         const unsigned long long *q_s = reinterpret_cast<const unsigned long long *>(gbase);
-        double ov2[2] = {0.0, 0.0};
+        Df ov2[2] = {df_zero(), df_zero()};
 #pragma unroll
         for (int t = 0; t < PT; ++t) {
             const int i = gt + 32 * kQ * t;
             // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
             const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q_s[i]), fixed_inv), ini_s[i]);
             const float o = __fsub_rn(d, coef);
-            ov2[t & 1] += (double)(o > 0.0f ? o : 0.0f);   // src/epotential.rs:274-276
+            ov2[t & 1] = df_add(ov2[t & 1], o > 0.0f ? o : 0.0f);   // src/epotential.rs:274-276
             v[t] = __fmul_rn(d, inv_area);                   // src/epotential.rs:284-285
         }
-        ovf = ov2[0] + ov2[1];
+        ovf = df_add(ov2[0], ov2[1]);
         if (zero_map) {
             ulonglong2 *zr = reinterpret_cast<ulonglong2 *>(dmap + (size_t)row * N);
 #pragma unroll
@@ -886,8 +884,7 @@ __global__ void __launch_bounds__(G * kQ * 32) k_rows_dct_g(
     float *out = t1 + (size_t)row * N;
     group_dct2_post<H>(xs, tb.tw, tb.ek, gt, [&](int k, float y) { out[k] = y; });
     if (from_map && partials) {
-        const double b = block_sum(ovf, shr);
-        double vals[1] = {b};
+        const Df vals[1] = {block_sum(ovf, shr)};
         if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_OVF], gridDim.x)) {
             const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
             if (threadIdx.x == 0) {
@@ -1000,7 +997,7 @@ __global__ void __launch_bounds__(G * kQ * 32) k_rows_inv_g(
 
 // The density map as rho for the tensor-core solve: the conversion of R1 (same
 // float rules, so rho is bit-identical to what the FFT path transforms), the
-// FP64 overflow sum with the last-block finalize, and the map zeroing.
+// double-float overflow sum with the last-block finalize, and the map zeroing.
 __global__ void __launch_bounds__(kThreads) k_map_rho(size_t mn, unsigned long long *__restrict__ dmap,
                                                       const float *__restrict__ initial, float fixed_inv, float coef,
                                                       float inv_area, int zero_map, float *__restrict__ rho,
@@ -1008,18 +1005,17 @@ __global__ void __launch_bounds__(kThreads) k_map_rho(size_t mn, unsigned long l
                                                       double movable_area) {
     __shared__ double shr[kThreads / 32];
     if (st->done) return;
-    double ovf = 0.0;
+    Df ovf = df_zero();
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < mn; idx += (size_t)gridDim.x * blockDim.x) {
         const unsigned long long q = dmap[idx];
         if (zero_map) dmap[idx] = 0ull;
         // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
         const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q), fixed_inv), initial[idx]);
         const float o = __fsub_rn(d, coef);
-        ovf += (double)(o > 0.0f ? o : 0.0f);    // src/epotential.rs:274-276
+        ovf = df_add(ovf, o > 0.0f ? o : 0.0f);  // src/epotential.rs:274-276
         rho[idx] = __fmul_rn(d, inv_area);         // src/epotential.rs:284-285
     }
-    const double b = block_sum(ovf, shr);
-    double vals[1] = {b};
+    const Df vals[1] = {block_sum(ovf, shr)};
     if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_OVF], gridDim.x)) {
         const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
         if (threadIdx.x == 0) {

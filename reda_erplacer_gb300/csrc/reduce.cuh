@@ -1,7 +1,14 @@
-// Deterministic reductions: FP64 block sums with a fixed thread->data mapping,
-// then a last-block finalize that sums the per-block partials in index order.
-// No block ever waits for another (the last block to arrive does the final
-// sum), so there is no spin-wait anywhere.
+// Deterministic reductions in double-float arithmetic.  A sum is carried as an
+// unevaluated pair hi + lo of FP32 values, renormalised after every addition
+// with Knuth's TwoSum and Dekker's FastTwoSum error-free transformations
+// (about 44 significant bits), and converted to FP64 once, at the end.  FP64
+// issues at a small fraction of the FP32 rate on this GPU: with FP64 block
+// sums every reduction tail was a long dependent chain on that pipe.
+//
+// Block sums use a fixed thread -> data mapping and shuffle tree; the block
+// that arrives last sums the per-block partials in index order.  No block ever
+// waits for another, so there is no spin-wait anywhere, and the result depends
+// only on the data and the grid.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -9,29 +16,73 @@
 
 namespace erp {
 
-// Sum of v over the block; result valid in thread 0.  sh: >= blockDim/32 doubles.
-__device__ __forceinline__ double block_sum(double v, double *sh) {
+struct Df {
+    float hi, lo;
+};
+// a partial slot (8 bytes, allocated as double) holds one pair
+static_assert(sizeof(Df) == sizeof(double), "partial slot size");
+
+__device__ __forceinline__ Df df_zero() { return Df{0.0f, 0.0f}; }
+
+// s + e == a + b exactly (round to nearest, no overflow)
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bv = __fsub_rn(s, a);
+    const float av = __fsub_rn(s, bv);
+    e = __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
+}
+
+// hi + lo == s + e, |lo| <= ulp(hi) / 2, for |s| >= |e|
+__device__ __forceinline__ Df fast_two_sum(float s, float e) {
+    const float hi = __fadd_rn(s, e);
+    return Df{hi, __fsub_rn(e, __fsub_rn(hi, s))};
+}
+
+__device__ __forceinline__ Df df_add(Df a, Df b) {
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    return fast_two_sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ Df df_add(Df a, float b) {
+    float s, e;
+    two_sum(a.hi, b, s, e);
+    return fast_two_sum(s, __fadd_rn(e, a.lo));
+}
+
+__device__ __forceinline__ double df_value(Df a) { return (double)a.hi + (double)a.lo; }
+
+__device__ __forceinline__ Df df_shfl_down(Df v, int o) {
+    return Df{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+}
+
+// Sum of v over the block; result valid in thread 0.  sh: >= blockDim/32 slots.
+__device__ __forceinline__ Df block_sum(Df v, double *sh) {
+    Df *shp = reinterpret_cast<Df *>(sh);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) v = df_add(v, df_shfl_down(v, o));
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
     __syncthreads();
-    if (l == 0) sh[w] = v;
+    if (l == 0) shp[w] = v;
     __syncthreads();
     if (w == 0) {
-        v = (l < nw) ? sh[l] : 0.0;
+        v = (l < nw) ? shp[l] : df_zero();
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        for (int o = 16; o > 0; o >>= 1) v = df_add(v, df_shfl_down(v, o));
     }
     return v;
 }
 
-// Thread 0 publishes `nv` values of this block into partials[slot*nv + k];
+__device__ __forceinline__ Df block_sum(float v, double *sh) { return block_sum(Df{v, 0.0f}, sh); }
+
+// Thread 0 publishes `nv` sums of this block into partial slots slot*nv + k;
 // returns true (in every thread) in the block that arrives last.
-__device__ __forceinline__ bool arrive_last(double *partials, int slot, int nv, const double *vals,
-                                            uint32_t *ctr, uint32_t nblocks) {
+__device__ __forceinline__ bool arrive_last(double *partials, int slot, int nv, const Df *vals, uint32_t *ctr,
+                                            uint32_t nblocks) {
     __shared__ int s_last;
     if (threadIdx.x == 0) {
-        for (int k = 0; k < nv; ++k) partials[(size_t)slot * nv + k] = vals[k];
+        Df *p = reinterpret_cast<Df *>(partials);
+        for (int k = 0; k < nv; ++k) p[(size_t)slot * nv + k] = vals[k];
         __threadfence();
         const uint32_t t = atomicAdd(ctr, 1u);
         s_last = (t == nblocks - 1);
@@ -42,12 +93,16 @@ __device__ __forceinline__ bool arrive_last(double *partials, int slot, int nv, 
     return last;
 }
 
-// In the last block: sum partials[k*nv + j] over k < count for value j (fixed order).
-__device__ __forceinline__ double sum_partials(const double *partials, int count, int nv, int j,
-                                               double *sh) {
-    double v = 0.0;
-    for (int k = threadIdx.x; k < count; k += blockDim.x) v += __ldcg(partials + (size_t)k * nv + j);
-    return block_sum(v, sh);
+// In the last block: the sum of partial slots k*nv + j over k < count (fixed
+// order), as FP64 in thread 0.
+__device__ __forceinline__ double sum_partials(const double *partials, int count, int nv, int j, double *sh) {
+    const float2 *p = reinterpret_cast<const float2 *>(partials);
+    Df v = df_zero();
+    for (int k = threadIdx.x; k < count; k += blockDim.x) {
+        const float2 q = __ldcg(p + (size_t)k * nv + j);
+        v = df_add(v, Df{q.x, q.y});
+    }
+    return df_value(block_sum(v, sh));
 }
 
 }  // namespace erp
