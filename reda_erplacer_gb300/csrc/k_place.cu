@@ -15,6 +15,7 @@
 #include <atomic>
 
 #include "erp_internal.cuh"
+#include "fixedpoint.h"
 #include "reduce.cuh"
 
 namespace erp {
@@ -445,7 +446,7 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
             for (int dy = 0; dy < ny; ++dy) {
                 const int by = byl + dy;
                 const float py = tri_clamped(yi, syi, by, bh);
-                const unsigned long long c = (unsigned long long)__float2ll_rn((px * py) * scale);
+                const unsigned long long c = (unsigned long long)fxp_rint_u64((px * py) * scale);
                 if (c) add(bx, by, c);
             }
         }

@@ -23,6 +23,7 @@
 // bit-reversed order out), twiddles from FP64-computed tables.
 #include "erp_internal.cuh"
 #include "bulk_copy.cuh"
+#include "fixedpoint.h"
 #include "reduce.cuh"
 
 namespace erp {
@@ -93,7 +94,7 @@ __global__ void __launch_bounds__(kThreads) k_rows_dct(
                 const unsigned long long q = dmap[k];
                 if (zero_map) dmap[k] = 0ull;
                 // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
-                const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q), fixed_inv), initial[k]);
+                const float d = __fadd_rn(__fmul_rn(fxp_u64_to_float(q), fixed_inv), initial[k]);
                 const float o = __fsub_rn(d, coef);
                 ovf = df_add(ovf, o > 0.0f ? o : 0.0f);    // src/epotential.rs:274-276
                 v[h] = __fmul_rn(d, inv_area);               // src/epotential.rs:284-285
@@ -520,7 +521,7 @@ __global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
         for (int t = 0; t < 2 * E; ++t) {
             const int i = lane + 32 * t;
             // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
-            const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q_s[i]), fixed_inv), ini_s[i]);
+            const float d = __fadd_rn(__fmul_rn(fxp_u64_to_float(q_s[i]), fixed_inv), ini_s[i]);
             const float o = __fsub_rn(d, coef);
             ov4[t & 3] = df_add(ov4[t & 3], o > 0.0f ? o : 0.0f);   // src/epotential.rs:274-276
             v[t] = __fmul_rn(d, inv_area);                    // src/epotential.rs:284-285
@@ -853,7 +854,7 @@ __global__ void __launch_bounds__(G * kQ * 32) k_rows_dct_g(
         for (int t = 0; t < PT; ++t) {
             const int i = gt + 32 * kQ * t;
             // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
-            const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q_s[i]), fixed_inv), ini_s[i]);
+            const float d = __fadd_rn(__fmul_rn(fxp_u64_to_float(q_s[i]), fixed_inv), ini_s[i]);
             const float o = __fsub_rn(d, coef);
             ov2[t & 1] = df_add(ov2[t & 1], o > 0.0f ? o : 0.0f);   // src/epotential.rs:274-276
             v[t] = __fmul_rn(d, inv_area);                   // src/epotential.rs:284-285
@@ -1010,7 +1011,7 @@ __global__ void __launch_bounds__(kThreads) k_map_rho(size_t mn, unsigned long l
         const unsigned long long q = dmap[idx];
         if (zero_map) dmap[idx] = 0ull;
         // d = (float)sum * 2^-S + initial  (src/density.rs:231-236, fixed point)
-        const float d = __fadd_rn(__fmul_rn(__ll2float_rn((long long)q), fixed_inv), initial[idx]);
+        const float d = __fadd_rn(__fmul_rn(fxp_u64_to_float(q), fixed_inv), initial[idx]);
         const float o = __fsub_rn(d, coef);
         ovf = df_add(ovf, o > 0.0f ? o : 0.0f);  // src/epotential.rs:274-276
         rho[idx] = __fmul_rn(d, inv_area);         // src/epotential.rs:284-285
