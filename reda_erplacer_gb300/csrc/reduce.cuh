@@ -1,9 +1,8 @@
-// Deterministic reductions in double-float arithmetic.  A sum is carried as an
-// unevaluated pair hi + lo of FP32 values, renormalised after every addition
-// with Knuth's TwoSum and Dekker's FastTwoSum error-free transformations
-// (about 44 significant bits), and converted to FP64 once, at the end.  FP64
-// issues at a small fraction of the FP32 rate on this GPU: with FP64 block
-// sums every reduction tail was a long dependent chain on that pipe.
+// Deterministic reductions in double-float arithmetic (dfloat.h): a sum is
+// carried as an unevaluated pair hi + lo of FP32 values, about 44 significant
+// bits, and converted to FP64 once, at the end.  FP64 issues at a small
+// fraction of the FP32 rate on this GPU: with FP64 block sums every reduction
+// tail was a long dependent chain on that pipe.
 //
 // Block sums use a fixed thread -> data mapping and shuffle tree; the block
 // that arrives last sums the per-block partials in index order.  No block ever
@@ -14,43 +13,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "dfloat.h"
+
 namespace erp {
 
-struct Df {
-    float hi, lo;
-};
 // a partial slot (8 bytes, allocated as double) holds one pair
 static_assert(sizeof(Df) == sizeof(double), "partial slot size");
-
-__device__ __forceinline__ Df df_zero() { return Df{0.0f, 0.0f}; }
-
-// s + e == a + b exactly (round to nearest, no overflow)
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-    s = __fadd_rn(a, b);
-    const float bv = __fsub_rn(s, a);
-    const float av = __fsub_rn(s, bv);
-    e = __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
-}
-
-// hi + lo == s + e, |lo| <= ulp(hi) / 2, for |s| >= |e|
-__device__ __forceinline__ Df fast_two_sum(float s, float e) {
-    const float hi = __fadd_rn(s, e);
-    return Df{hi, __fsub_rn(e, __fsub_rn(hi, s))};
-}
-
-__device__ __forceinline__ Df df_add(Df a, Df b) {
-    float s, e;
-    two_sum(a.hi, b.hi, s, e);
-    return fast_two_sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
-}
-
-__device__ __forceinline__ Df df_add(Df a, float b) {
-    float s, e;
-    two_sum(a.hi, b, s, e);
-    return fast_two_sum(s, __fadd_rn(e, a.lo));
-}
-
-__device__ __forceinline__ double df_value(Df a) { return (double)a.hi + (double)a.lo; }
 
 __device__ __forceinline__ Df df_shfl_down(Df v, int o) {
     return Df{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
