@@ -15,6 +15,7 @@
 #include <atomic>
 
 #include "erp_internal.cuh"
+#include "binrange.h"
 #include "fixedpoint.h"
 #include "reduce.cuh"
 
@@ -614,12 +615,6 @@ __device__ __forceinline__ float tri_raw(float x, float s, int k, float bs) {
     return fminf(x + s, bin_xl + bs) - fmaxf(x, bin_xl);
 }
 
-// Rust `f.to_isize().unwrap_or(0)`: truncation; NaN / out of range -> 0
-__device__ __forceinline__ long long to_isize0(float v) {
-    if (!(v == v) || v >= 9.2e18f || v <= -9.2e18f) return 0;
-    return (long long)v;
-}
-
 // compute_electric_force (src/eforce.rs:15-91)
 __global__ void __launch_bounds__(kThreads) k_force(
     int NM, const int32_t *__restrict__ perm, const float2 *__restrict__ xy, const float4 *__restrict__ soff,
@@ -633,19 +628,15 @@ __global__ void __launch_bounds__(kThreads) k_force(
     if (st->done) return;
     // the field gathered over cell i's bins (src/eforce.rs)
     auto force = [&](int i, float nx, float ny, float sx, float sy, float r) {
-        long long xl = to_isize0((nx - 0.0f) * inv_bw);
-        if (xl < 0) xl = 0;
-        long long xh = to_isize0((nx + sx - 0.0f) * inv_bw) + 1;
-        if (xh < 0 || xh > m) xh = m;     // a negative end wraps to usize::MAX, then min
-        long long yl = to_isize0((ny - 0.0f) * inv_bh);
-        if (yl < 0) yl = 0;
-        long long yh = to_isize0((ny + sy - 0.0f) * inv_bh) + 1;
-        if (yh < 0 || yh > n) yh = n;
+        const int xl = force_bin_lo((nx - 0.0f) * inv_bw, m);
+        const int xh = force_bin_hi((nx + sx - 0.0f) * inv_bw, m);
+        const int yl = force_bin_lo((ny - 0.0f) * inv_bh, n);
+        const int yh = force_bin_hi((ny + sy - 0.0f) * inv_bh, n);
         float gx = 0.0f, gy = 0.0f;
-        for (int k = (int)xl; k < (int)xh; ++k) {
+        for (int k = xl; k < xh; ++k) {
             const float px = tri_raw(nx, sx, k, bw);
             const float *rx = fx + (size_t)k * n, *ry = fy + (size_t)k * n;
-            for (int hh = (int)yl; hh < (int)yh; ++hh) {
+            for (int hh = yl; hh < yh; ++hh) {
                 const float py = tri_raw(ny, sy, hh, bh);
                 const float area = px * py;
                 gx += area * __ldg(rx + hh);
@@ -940,17 +931,24 @@ __global__ void k_scheduler(int use_args, float hpwl_arg, float ovf_arg, SchedLo
     const int it1 = st->iteration + 1;
     const float ref0 = st->hpwl_init_set ? st->hpwl_init : hpwl;
     const float delta0 = hpwl - st->hpwl_cur;   // hpwl_cur - hpwl_prev after the update below
-    double lnb, ex;
+    // exponents: (ovf - 0.1) * 20 / 9 - 1 (lane 1), iteration, or -delta / ref,
+    // each as num / den in the same operation order, so one convergent division
+    double lnb, num, den;
     if (lane == 1) {
         lnb = lg.ln_ten;
-        ex = ((double)ovf - 0.1) * 20.0 / 9.0 - 1.0;
+        num = ((double)ovf - 0.1) * 20.0;
+        den = 9.0;
     } else if (delta0 < 0.0f) {
         lnb = lg.ln_shrink;
-        ex = (double)it1;
+        num = (double)it1;
+        den = 1.0;
     } else {
         lnb = lg.ln_grow;
-        ex = -(double)delta0 / (double)ref0;
+        num = -(double)delta0;
+        den = (double)ref0;
     }
+    double ex = num / den;
+    if (lane == 1) ex -= 1.0;
     double pw = exp(ex * lnb);
     if (lane == 1) pw = pw < 0.05 ? 0.05 : (pw > 10.0 ? 10.0 : pw);
     else if (delta0 < 0.0f) pw = pw < 0.98 ? 0.98 : pw;
