@@ -4,6 +4,10 @@
   device (non-finite HPWL, overflow or step length): the host reads ERP_ENAN,
   and the context stays retired.  Every index the kernels derive from a
   position is clamped, so NaN coordinates read and write in bounds.
+* Positions far outside the die (beyond 2^31 bins, negative, huge) index
+  nothing out of bounds: every kernel clamps the bins it derives from a
+  position, so the step ends with a status (ERP_OK, or ERP_ENAN if a total
+  overflowed), never a CUDA error, and the device stays usable.
 * Inside the server a job that cannot be set up (a bin grid the library
   rejects, a non-finite coordinate) fails alone on its admission worker: its
   result carries its status, and the other jobs of the stream finish with the
@@ -71,3 +75,28 @@ def test_server_isolates_failed_jobs(R):
         with R.Placement(d, b, 1.0, start_mode=1) as pl:
             it, last = pl.run(60)
         assert r["last"]["hpwl"] == last["hpwl"] and r["last"]["overflow"] == last["overflow"]
+
+
+def test_out_of_range_positions_stay_in_bounds(R):
+    d = small_synth(3000, seed=43)
+    with R.Placement(d, (64, 64), 1.0, start_mode=1) as pl:
+        pl.step()
+        x, y = pl.positions()
+        x[3], y[3] = 3.0e9, 5.0            # beyond 2^31 bins of the grid in x
+        x[4], y[4] = -4.0e12, -7.0e10      # far below the die
+        x[8], y[8] = 1.0e20, 1.0e20        # beyond isize in bin units
+        pl.set_positions(x, y)
+        try:
+            for _ in range(3):
+                pl.step()
+            status = 0
+        except R.ErpError as e:
+            status = e.status
+        assert status in (0, R.lib.ENAN)
+        if status == 0:   # the update clamps every cell back onto the die
+            x2, y2 = pl.positions()
+            NM = d.num_movable
+            assert np.all(np.isfinite(x2[:NM])) and np.all(x2[:NM] >= 0.0) and np.all(x2[:NM] <= d.die_w)
+    with R.Placement(d, (64, 64), 1.0, start_mode=1) as pl:
+        it, last = pl.run(5)
+        assert it == 5 and np.isfinite(last["hpwl"])
