@@ -146,7 +146,11 @@ erp_status erp_step(erp_ctx *ctx, erp_step_stats *stats);
 
 /* Drop-in form for a host that owns the coordinates (the reference's
  * ps.instances, mutated by step_adaptive, src/nesterov.rs:39): copies x/y
- * (all nodes) to the device, runs one step, copies the new x/y back. */
+ * (all nodes) to the device, runs one step, copies the new x/y back.  When x
+ * and y each lie in one page-locked allocation (cudaHostAlloc or
+ * cudaHostRegister) that covers all nodes, the device reads and writes them
+ * directly instead; an array whose first or last element is not page-locked
+ * goes through copies. */
 erp_status erp_step_host(erp_ctx *ctx, float *x, float *y, erp_step_stats *stats);
 
 /* Run up to max_iterations steps (the CLI loop, src/main.rs:78-90), stopping

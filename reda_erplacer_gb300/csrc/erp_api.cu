@@ -639,13 +639,22 @@ extern "C" erp_status erp_step(erp_ctx *ctx, erp_step_stats *stats) {
 
 // The device address of a registered (pinned, device-mapped) host buffer, or
 // nullptr for any other memory.
-static float *mapped_host(float *p) {
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+// p[0, n) as device-mapped host memory (registered or cudaHostAlloc'd), or
+// nullptr.  Both the first and the last element must be mapped, contiguously,
+// so a registration shorter than the array falls back to copies instead of the
+// device running past it.  (A range that starts and ends in two different
+// registrations with unregistered memory between them is not detected: the
+// caller's contract is one registration per array.)
+static float *mapped_host(float *p, int n) {
+    if (n <= 0) return nullptr;
+    cudaPointerAttributes a, b;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess || cudaPointerGetAttributes(&b, p + (n - 1)) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    return a.type == cudaMemoryTypeHost ? static_cast<float *>(a.devicePointer) : nullptr;
+    if (a.type != cudaMemoryTypeHost || b.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    float *d = static_cast<float *>(a.devicePointer);
+    return b.devicePointer == static_cast<void *>(d + (n - 1)) ? d : nullptr;
 }
 
 extern "C" erp_status erp_step_host(erp_ctx *ctx, float *x, float *y, erp_step_stats *stats) {
@@ -653,7 +662,7 @@ extern "C" erp_status erp_step_host(erp_ctx *ctx, float *x, float *y, erp_step_s
     if (!x || !y) return ERP_EINVAL;
     // Registered host buffers are read and written by the device itself (one pass
     // each way, no staging); other host memory goes through copies.
-    float *dx = mapped_host(x), *dy = mapped_host(y);
+    float *dx = mapped_host(x, c.N), *dy = mapped_host(y, c.N);
     const bool direct = dx && dy;
     if (direct) {
         launch_xy_from_host(c, dx, dy);
