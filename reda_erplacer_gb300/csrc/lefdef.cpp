@@ -52,6 +52,17 @@ struct Fail : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
 
+// Every coordinate and size in database units (DEF units, LEF grid units) is
+// limited to |v| <= 2^40 (about 1.1e12 units, far beyond any die), so sums and
+// differences of a few of them never overflow int64.
+constexpr double kMaxUnits = 1099511627776.0;
+
+// llround(v) for a quantity in database units, or Fail.
+int64_t to_units(double v, const char *what) {
+    if (!std::isfinite(v) || std::fabs(v) > kMaxUnits) throw Fail(std::string(what) + " out of range");
+    return (int64_t)std::llround(v);
+}
+
 enum Kind : uint8_t { kMovable = 0, kFixed = 1, kIo = 2 };
 enum Orient : uint8_t { oN = 0, oW, oS, oE, oFN, oFW, oFS, oFE };
 const char *const kOrientName[8] = {"N", "W", "S", "E", "FN", "FW", "FS", "FE"};
@@ -260,7 +271,7 @@ struct Lex {
     }
     int64_t inum() {
         const double v = num();
-        if (!std::isfinite(v) || std::fabs(v) > 4e18) fail("number out of range");
+        if (!std::isfinite(v) || std::fabs(v) > kMaxUnits) fail("number out of range");
         return (int64_t)std::llround(v);
     }
     void skip_statement() {   // to the next ';' token (inclusive)
@@ -667,12 +678,12 @@ void finalize(erp_netlist &nl) {
     const int64_t G = nl.lef_dbu > 0 ? nl.lef_dbu : D;
     nl.grid = G;
     for (Macro &m : nl.macros) {
-        m.W = std::llround(m.w * (double)G);
-        m.H = std::llround(m.h * (double)G);
+        m.W = to_units(m.w * (double)G, "macro size");
+        m.H = to_units(m.h * (double)G, "macro size");
         for (MacroPin &p : m.pins) {
             if (p.has) {
-                p.c2x = std::llround((p.lx + p.hx + 2.0 * m.ox) * (double)G);
-                p.c2y = std::llround((p.ly + p.hy + 2.0 * m.oy) * (double)G);
+                p.c2x = to_units((p.lx + p.hx + 2.0 * m.ox) * (double)G, "pin shape");
+                p.c2y = to_units((p.ly + p.hy + 2.0 * m.oy) * (double)G, "pin shape");
             } else {
                 p.c2x = m.W;
                 p.c2y = m.H;
@@ -849,7 +860,8 @@ void write_lef(const erp_netlist &nl, const char *path) {
     o.put("LAYER metal1\n  TYPE ROUTING ;\n  DIRECTION HORIZONTAL ;\nEND metal1\n\n");
     if (nl.site_w > 0 && nl.row_h > 0)
         o.printf("SITE %s\n  CLASS CORE ;\n  SYMMETRY Y ;\n  SIZE %s BY %s ;\nEND %s\n\n", nl.site_name.c_str(),
-                 um(std::llround(nl.site_w * (double)G), G).c_str(), um(std::llround(nl.row_h * (double)G), G).c_str(),
+                 um(to_units(nl.site_w * (double)G, "site width"), G).c_str(),
+                 um(to_units(nl.row_h * (double)G, "row height"), G).c_str(),
                  nl.site_name.c_str());
     for (const Macro &m : nl.macros) {
         o.printf("MACRO %s\n  CLASS %s ;\n  ORIGIN 0 0 ;\n  SIZE %s BY %s ;\n  SYMMETRY X Y ;\n", m.name.c_str(),
@@ -883,9 +895,11 @@ void write_def(const erp_netlist &nl, const char *path, const int64_t *xs, const
     o.printf("DIEAREA ( %lld %lld ) ( %lld %lld ) ;\n\n", (long long)nl.die[0], (long long)nl.die[1],
              (long long)nl.die[2], (long long)nl.die[3]);
     if (nl.site_w > 0 && nl.row_h > 0) {
-        const int64_t step = std::llround(nl.site_w * (double)D), rh = std::llround(nl.row_h * (double)D);
+        const int64_t step = to_units(nl.site_w * (double)D, "site width");
+        const int64_t rh = to_units(nl.row_h * (double)D, "row height");
         if (step > 0 && rh > 0) {
             const int64_t sites = (nl.die[2] - nl.die[0]) / step, rows = (nl.die[3] - nl.die[1]) / rh;
+            if (rows > (int64_t(1) << 24)) throw Fail("row height too small for the die: more than 2^24 rows");
             for (int64_t r = 0; r < rows; ++r)
                 o.printf("ROW ROW_%lld %s %lld %lld %s DO %lld BY 1 STEP %lld 0 ;\n", (long long)r, nl.site_name.c_str(),
                          (long long)nl.die[0], (long long)(nl.die[1] + r * rh), (r & 1) ? "FS" : "N", (long long)sites,
@@ -1013,12 +1027,12 @@ extern "C" erp_status erp_netlist_from_design(const erp_design *d, const erp_lef
         nl->site_w = p && p->site_w > 0 ? p->site_w : 0;
         nl->row_h = p && p->row_h > 0 ? p->row_h : 0;
         nl->die[0] = nl->die[1] = 0;
-        nl->die[2] = std::llround((double)d->die_w * (double)D);
-        nl->die[3] = std::llround((double)d->die_h * (double)D);
+        nl->die[2] = to_units((double)d->die_w * (double)D, "die size");
+        nl->die[3] = to_units((double)d->die_h * (double)D, "die size");
         nl->have_die = true;
         auto q = [&](float v) -> int64_t {
             if (!std::isfinite(v)) throw Fail("non-finite coordinate in design");
-            return std::llround((double)v * (double)D);
+            return to_units((double)v * (double)D, "coordinate");
         };
         // slot of each pin in its instance's list: the macro pin P<slot>
         std::vector<int32_t> slot(P, -1);
@@ -1195,8 +1209,8 @@ extern "C" erp_status erp_def_write_placed(const erp_netlist *nl, const float *x
         for (int32_t k = 0; k < nl->num_movable; ++k) {
             if (!std::isfinite(x[k]) || !std::isfinite(y[k])) throw Fail("non-finite position of instance " + std::to_string(k));
             const int32_t i = nl->order[k];
-            xs[i] = std::llround((double)x[k] * D) + nl->die[0];
-            ys[i] = std::llround((double)y[k] * D) + nl->die[1];
+            xs[i] = to_units((double)x[k] * D, "position") + nl->die[0];
+            ys[i] = to_units((double)y[k] * D, "position") + nl->die[1];
         }
         if (nl->from_design) write_def(*nl, def_path, xs.data(), ys.data());
         else splice_def(*nl, def_path, xs.data(), ys.data());

@@ -22,7 +22,7 @@ from .design import Design
 def _check(st):
     if st != L.OK:
         msg = L.load().erp_lefdef_last_error()
-        raise L.ErpError(st, msg.decode() if msg else "")
+        raise L.ErpError(st, msg.decode(errors="replace") if msg else "")
 
 
 def _path(p):
@@ -67,13 +67,13 @@ class Netlist:
         r = self.lib.erp_netlist_node_name(self.h, int(i))
         if r is None:
             raise IndexError(i)
-        return r.decode()
+        return r.decode(errors="surrogateescape")   # names are bytes in the files
 
     def net_name(self, e):
         r = self.lib.erp_netlist_net_name(self.h, int(e))
         if r is None:
             raise IndexError(e)
-        return r.decode()
+        return r.decode(errors="surrogateescape")
 
     def write(self, lef_path=None, def_path=None):
         _check(self.lib.erp_lefdef_write(self.h, _path(lef_path) if lef_path else None,

@@ -203,4 +203,4 @@ def status_string(s):
 def check(status, ctx=None):
     if status != OK:
         msg = load().erp_last_error(ctx)
-        raise ErpError(status, msg.decode() if msg else "")
+        raise ErpError(status, msg.decode(errors="replace") if msg else "")

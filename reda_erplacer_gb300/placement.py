@@ -230,7 +230,7 @@ class Batch:
         last = (L.StepStats * self.K)()
         st = self.lib.erp_batch_run(self.h, int(max_iterations), float(stop_overflow), it, last)
         if st != L.OK:
-            raise L.ErpError(st, self.lib.erp_batch_last_error(self.h).decode())
+            raise L.ErpError(st, self.lib.erp_batch_last_error(self.h).decode(errors="replace"))
         return [int(v) for v in it], [s.as_dict() for s in last]
 
     def tuning(self):

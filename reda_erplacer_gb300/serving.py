@@ -22,7 +22,7 @@ class Server:
 
     def _ck(self, st):
         if st != L.OK:
-            raise L.ErpError(st, self.lib.erp_server_last_error(self.h).decode())
+            raise L.ErpError(st, self.lib.erp_server_last_error(self.h).decode(errors="replace"))
 
     def submit(self, job_id, design, num_bins, target_density=1.0, start_mode=L.START_DB):
         s = design.to_struct()
