@@ -15,7 +15,8 @@
 //    net of three or more pins (so the two-pin share is kept);
 //  * macros: each macro_area_frac of the die, aspect ratio uniform 0.5-2,
 //    positions uniform without overlap (rejection sampling);
-//  * die: square, area = cell area / (utilization * (1 - macro share));
+//  * die: square, area = cell area / (utilization * (1 - macro share)), its
+//    side at least the largest cell width or height;
 //  * start: die centre minus half the cell size plus Gaussian jitter
 //    (sigma = jitter_frac * die width), clamped onto the die.
 // Randomness: xoshiro256** seeded through splitmix64; only integer ops and
@@ -73,14 +74,37 @@ struct erp_synth {
     float die_w = 0, die_h = 0, util = 0, mov_area = 0;
 };
 
+namespace {
+bool positive(float v) { return v > 0.0f && std::isfinite(v); }   // false for NaN
+}  // namespace
+
+static erp_status synth_fill(const erp_synth_params *p, erp_synth *s);
+
 extern "C" erp_status erp_synth_create(const erp_synth_params *p, erp_synth **out) {
     if (!p || !out || p->num_cells < 2 || p->num_nets < 1 || p->num_io < 0 || p->num_macros < 0 ||
-        p->utilization <= 0 || p->site_w <= 0 || p->row_h <= 0 || p->min_sites < 1 ||
-        p->max_sites < p->min_sites || p->macro_area_frac < 0 ||
-        p->num_macros * (double)p->macro_area_frac >= 0.9)
+        !positive(p->utilization) || !positive(p->site_w) || !positive(p->row_h) || p->min_sites < 1 ||
+        p->max_sites < p->min_sites || !(p->macro_area_frac >= 0.0f) || !std::isfinite(p->macro_area_frac) ||
+        !std::isfinite(p->jitter_frac) || p->num_macros * (double)p->macro_area_frac >= 0.9)
         return ERP_EINVAL;
+    // node ids are int32 in erp_design
+    if ((int64_t)p->num_cells + p->num_macros + p->num_io >= INT32_MAX) return ERP_EINVAL;
     erp_synth *s = new (std::nothrow) erp_synth();
     if (!s) return ERP_ENOMEM;
+    erp_status st;
+    try {
+        st = synth_fill(p, s);
+    } catch (const std::bad_alloc &) {
+        st = ERP_ENOMEM;
+    }
+    if (st != ERP_OK) {
+        delete s;
+        return st;
+    }
+    *out = s;
+    return ERP_OK;
+}
+
+static erp_status synth_fill(const erp_synth_params *p, erp_synth *s) {
     Rng rng((uint64_t)p->seed);
     const int NC = p->num_cells, NMAC = p->num_macros, NIO = p->num_io, E = p->num_nets;
     const int N = NC + NMAC + NIO;
@@ -98,6 +122,12 @@ extern "C" erp_status erp_synth_create(const erp_synth_params *p, erp_synth **ou
     double macro_share = NMAC * (double)p->macro_area_frac;
     double die_area = cell_area / ((double)p->utilization * (1.0 - macro_share));
     double side = std::sqrt(die_area);
+    double max_dim = 0;   // a die narrower than a cell is unplaceable (only tiny designs reach this)
+    for (int i = 0; i < NC; ++i) max_dim = std::max(max_dim, (double)std::max(s->w[i], s->h[i]));
+    if (side < max_dim) {
+        side = max_dim;
+        die_area = side * side;
+    }
     s->die_w = s->die_h = (float)side;
     // macros
     std::vector<double> mx, my, mw, mh;
@@ -167,9 +197,12 @@ extern "C" erp_status erp_synth_create(const erp_synth_params *p, erp_synth **ou
     s->num_nets = E;
     s->n_2nets = 0;
     for (int e = 0; e < E && deg[e] == 2 && extra[e] == 0; ++e) s->n_2nets++;
+    int64_t P64 = 0;   // pin ids are int32 in erp_design
+    for (int e = 0; e < E; ++e) P64 += deg[e] + extra[e];
+    if (P64 >= INT32_MAX) return ERP_EINVAL;
     s->net_ptr.assign(E + 1, 0);
     for (int e = 0; e < E; ++e) s->net_ptr[e + 1] = s->net_ptr[e] + deg[e] + extra[e];
-    int P = s->net_ptr[E];
+    const int P = s->net_ptr[E];
     s->num_pins = P;
     s->net_pins.resize(P);
     s->pin_inst.resize(P);
@@ -211,7 +244,6 @@ extern "C" erp_status erp_synth_create(const erp_synth_params *p, erp_synth **ou
     for (int i = 0; i < N; ++i) s->npins[i] = (float)(s->inst_ptr[i + 1] - s->inst_ptr[i]);
     s->mov_area = (float)cell_area;
     s->util = (float)(cell_area / (die_area - macro_area));
-    *out = s;
     return ERP_OK;
 }
 
