@@ -122,7 +122,7 @@ erp_status validate(const erp_design *d, std::string &err) {
     REQ(d->num_nodes == 0 || (d->x && d->y && d->w && d->h && d->num_pins_f), "instance arrays missing");
     REQ(d->num_pins == 0 || (d->pin_ox && d->pin_oy && d->pin_inst), "pin arrays missing");
     REQ(d->net_ptr && d->inst_pin_ptr, "CSR pointers missing");
-    REQ(d->die_w > 0 && d->die_h > 0, "die must have positive size");
+    REQ(d->die_w > 0 && d->die_h > 0 && isfinite(d->die_w) && isfinite(d->die_h), "die must have positive, finite size");
     REQ(d->net_ptr[0] == 0, "net_ptr[0] must be 0");
     for (int e = 0; e < d->num_nets; ++e) REQ(d->net_ptr[e + 1] >= d->net_ptr[e], "net_ptr not monotone");
     REQ(d->net_ptr[d->num_nets] == 0 || d->net_pins, "net_pins missing");
@@ -134,14 +134,25 @@ erp_status validate(const erp_design *d, std::string &err) {
         REQ(!seen[p], "a pin belongs to more than one net");
         seen[p] = 1;
     }
-    for (int p = 0; p < d->num_pins; ++p) REQ(d->pin_inst[p] >= 0 && d->pin_inst[p] < d->num_nodes, "pin_inst out of range");
+    for (int p = 0; p < d->num_pins; ++p) {
+        REQ(d->pin_inst[p] >= 0 && d->pin_inst[p] < d->num_nodes, "pin_inst out of range");
+        REQ(isfinite(d->pin_ox[p]) && isfinite(d->pin_oy[p]), "non-finite pin offset");
+    }
     REQ(d->inst_pin_ptr[0] == 0, "inst_pin_ptr[0] must be 0");
     for (int i = 0; i < d->num_nodes; ++i) REQ(d->inst_pin_ptr[i + 1] >= d->inst_pin_ptr[i], "inst_pin_ptr not monotone");
     REQ(d->inst_pin_ptr[d->num_nodes] == 0 || d->inst_pins, "inst_pins missing");
-    for (int k = 0; k < d->inst_pin_ptr[d->num_nodes]; ++k)
-        REQ(d->inst_pins[k] >= 0 && d->inst_pins[k] < d->num_pins, "inst pin id out of range");
+    std::fill(seen.begin(), seen.end(), 0);
+    for (int k = 0; k < d->inst_pin_ptr[d->num_nodes]; ++k) {   // macro_2_pins lists each pin once
+        const int p = d->inst_pins[k];
+        REQ(p >= 0 && p < d->num_pins, "inst pin id out of range");
+        REQ(!seen[p], "a pin is listed twice in inst_pins");
+        seen[p] = 1;
+    }
     for (int i = 0; i < d->num_nodes; ++i) {
-        REQ(isfinite(d->x[i]) && isfinite(d->y[i]) && d->w[i] >= 0 && d->h[i] >= 0, "non-finite or negative instance geometry");
+        REQ(isfinite(d->x[i]) && isfinite(d->y[i]) && d->w[i] >= 0 && d->h[i] >= 0 && isfinite(d->w[i]) &&
+                isfinite(d->h[i]),
+            "non-finite or negative instance geometry");
+        REQ(d->num_pins_f[i] >= 0 && isfinite(d->num_pins_f[i]), "non-finite or negative num_pins_f");
         for (int k = d->inst_pin_ptr[i]; k < d->inst_pin_ptr[i + 1]; ++k)
             REQ(d->pin_inst[d->inst_pins[k]] == i, "inst_pins disagrees with pin_inst");
     }
@@ -237,6 +248,16 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     }
     erp_status s = validate(d, c.err);
     if (s != ERP_OK) return s;
+    c.target_density = prm.target_density >= 0 ? prm.target_density : d->cell_utilization;
+    if (!(c.target_density > 0) || !isfinite(c.target_density)) {
+        c.err = "target density (or the design's cell_utilization) must be positive and finite";
+        return ERP_EINVAL;
+    }
+    c.movable_area = d->movable_area;
+    if (!(c.movable_area > 0) || !isfinite(c.movable_area)) {
+        c.err = "movable_area must be positive and finite";
+        return ERP_EINVAL;
+    }
     s = check_device(prm.device, c.err);
     if (s != ERP_OK) return s;
     c.device = prm.device;
@@ -255,12 +276,6 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     c.inv_bh = 1.0f / c.bin_h;
     c.bin_area = c.bin_w * c.bin_h;
     c.inv_bin_area = 1.0f / c.bin_area;
-    c.target_density = prm.target_density >= 0 ? prm.target_density : d->cell_utilization;
-    c.movable_area = d->movable_area;
-    if (!(c.movable_area > 0)) {
-        c.err = "movable_area must be positive";
-        return ERP_EINVAL;
-    }
     if (prm.stream) {
         c.stream = (cudaStream_t)prm.stream;
         c.own_stream = false;

@@ -71,6 +71,51 @@ def test_invalid_designs_rejected(R):
     assert e.value.status == R.lib.EINVAL
 
 
+def test_non_finite_and_malformed_inputs_rejected(R):
+    """Validation runs before the device check, so these fail with ERP_EINVAL
+    and a message whether or not a GPU is present."""
+    import copy
+
+    def variant(f):
+        d = copy.deepcopy(edge_design())
+        f(d)
+        return d
+
+    def set_item(name, i, v):
+        def f(d):
+            a = getattr(d, name).copy()
+            a[i] = v
+            setattr(d, name, a)
+        return f
+
+    cases = [
+        ("instance width", set_item("w", 1, np.inf), {}, "instance geometry"),
+        ("instance height", set_item("h", 0, np.nan), {}, "instance geometry"),
+        ("pin offset", set_item("pin_ox", 2, np.nan), {}, "pin offset"),
+        ("pin count", set_item("num_pins_f", 0, np.nan), {}, "num_pins_f"),
+        ("negative pin count", set_item("num_pins_f", 1, -1.0), {}, "num_pins_f"),
+        ("die", lambda d: setattr(d, "die_w", float("inf")), {}, "die"),
+        ("movable area", lambda d: setattr(d, "movable_area", float("inf")), {}, "movable_area"),
+        ("target density", lambda d: None, {"target_density": float("inf")}, "target density"),
+        ("cell utilisation", lambda d: setattr(d, "cell_utilization", float("nan")), {"target_density": -1.0},
+         "target density"),
+        ("pin listed twice", set_item("inst_pins", 1, None), {}, "inst_pins"),
+    ]
+    for what, f, kw, msg in cases:
+        if what == "pin listed twice":
+            def f(d):
+                a = d.inst_pins.copy()
+                i = int(np.argmax(np.diff(d.inst_pin_ptr) >= 2))   # an instance with two pins
+                k = d.inst_pin_ptr[i]
+                a[k + 1] = a[k]
+                d.inst_pins = a
+        d = variant(f)
+        with pytest.raises(R.ErpError) as e:
+            R.Placement(d, (32, 16), **({"target_density": 1.0} | kw))
+        assert e.value.status == R.lib.EINVAL, what
+        assert msg in str(e.value), (what, str(e.value))
+
+
 def test_synth_is_deterministic_and_follows_rule(R):
     a = R.synth(5000, 5250, num_io=100, num_macros=4, utilization=0.65, seed=42)
     b = R.synth(5000, 5250, num_io=100, num_macros=4, utilization=0.65, seed=42)
