@@ -248,8 +248,9 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     }
     erp_status s = validate(d, c.err);
     if (s != ERP_OK) return s;
+    // target_density < 0 selects the design's cell_utilization; NaN is an error
     c.target_density = prm.target_density >= 0 ? prm.target_density : d->cell_utilization;
-    if (!(c.target_density > 0) || !isfinite(c.target_density)) {
+    if (isnan(prm.target_density) || !(c.target_density > 0) || !isfinite(c.target_density)) {
         c.err = "target density (or the design's cell_utilization) must be positive and finite";
         return ERP_EINVAL;
     }

@@ -17,7 +17,9 @@
 
 #include <sys/stat.h>
 
+#include <cerrno>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -65,6 +67,28 @@ struct Args {
     int device = 0;
 };
 
+// a whole-token number, or exit 2 (strtol / strtof alone take "12abc" as 12
+// and "abc" as 0)
+long whole_int(const std::string &k, const char *v) {
+    char *end = nullptr;
+    errno = 0;
+    const long r = std::strtol(v, &end, 10);
+    if (end == v || *end || errno) {
+        std::fprintf(stderr, "error: %s wants an integer, got '%s'\n", k.c_str(), v);
+        std::exit(2);
+    }
+    return r;
+}
+float whole_float(const std::string &k, const char *v) {
+    char *end = nullptr;
+    const float r = std::strtof(v, &end);
+    if (end == v || *end || !std::isfinite(r)) {
+        std::fprintf(stderr, "error: %s wants a finite number, got '%s'\n", k.c_str(), v);
+        std::exit(2);
+    }
+    return r;
+}
+
 int parse(int argc, char **argv, Args &a) {
     for (int i = 1; i < argc; ++i) {
         const std::string k = argv[i];
@@ -77,16 +101,17 @@ int parse(int argc, char **argv, Args &a) {
         };
         if (k == "-d" || k == "--def") a.def = val("a file");
         else if (k == "-l" || k == "--lef") a.lef.push_back(val("a file"));
-        else if (k == "--iterations") a.iterations = std::strtol(val("a count"), nullptr, 10);
+        else if (k == "--iterations") a.iterations = whole_int(k, val("a count"));
         else if (k == "-v" || k == "--verbose") a.verbose = true;
         else if (k == "--bins") {
             const char *v = val("MxN");
-            if (std::sscanf(v, "%dx%d", &a.m, &a.n) != 2) {
+            char tail = 0;
+            if (std::sscanf(v, "%dx%d%c", &a.m, &a.n, &tail) != 2) {
                 std::fprintf(stderr, "error: --bins wants MxN, got '%s'\n", v);
                 return 2;
             }
-        } else if (k == "--target-density") a.target_density = std::strtof(val("a value"), nullptr);
-        else if (k == "--stop-overflow") a.stop_overflow = std::strtof(val("a value"), nullptr);
+        } else if (k == "--target-density") a.target_density = whole_float(k, val("a value"));
+        else if (k == "--stop-overflow") a.stop_overflow = whole_float(k, val("a value"));
         else if (k == "--precision") {
             const std::string v = val("fp32|tf32|bf16x3");
             if (v == "fp32") a.precision = ERP_PREC_FP32;
@@ -106,7 +131,7 @@ int parse(int argc, char **argv, Args &a) {
             }
         } else if (k == "--out") a.out = val("a file");
         else if (k == "--images") a.images = val("a directory");
-        else if (k == "--device") a.device = (int)std::strtol(val("an index"), nullptr, 10);
+        else if (k == "--device") a.device = (int)whole_int(k, val("an index"));
         else if (k == "-h" || k == "--help") {
             usage(stdout);
             std::exit(0);
@@ -130,6 +155,7 @@ int parse(int argc, char **argv, Args &a) {
 }  // namespace
 
 int main(int argc, char **argv) {
+    std::setvbuf(stdout, nullptr, _IOLBF, 0);   // a redirected log keeps the order of the INFO and error lines
     Args a;
     if (int rc = parse(argc, argv, a)) return rc;
     if (a.images.empty() && is_dir("images")) a.images = "images";

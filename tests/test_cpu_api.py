@@ -97,6 +97,7 @@ def test_non_finite_and_malformed_inputs_rejected(R):
         ("die", lambda d: setattr(d, "die_w", float("inf")), {}, "die"),
         ("movable area", lambda d: setattr(d, "movable_area", float("inf")), {}, "movable_area"),
         ("target density", lambda d: None, {"target_density": float("inf")}, "target density"),
+        ("NaN target density", lambda d: None, {"target_density": float("nan")}, "target density"),
         ("cell utilisation", lambda d: setattr(d, "cell_utilization", float("nan")), {"target_density": -1.0},
          "target density"),
         ("pin listed twice", set_item("inst_pins", 1, None), {}, "inst_pins"),

@@ -237,3 +237,24 @@ def test_cli_reads_and_fails_loudly_without_a_gpu(R, built, tmp_path):
     assert "sm_103" in r.stderr or "no CUDA" in r.stderr or "device" in r.stderr
     r = subprocess.run([build.CLI, "-d", DEF], capture_output=True, text=True, timeout=60)
     assert r.returncode == 2 and "usage" in r.stderr
+
+
+def test_cli_rejects_bad_arguments_and_inputs(R, built, tmp_path):
+    """Flag errors exit 2 with usage; unreadable inputs and parameters the library
+    rejects exit 1 with the reason, before any device work (GPU or not)."""
+    from reda_erplacer_gb300 import build
+    base = [build.CLI, "-l", TECH, "-l", CELLS, "-d", DEF]
+    usage = [["--bogus"], ["--precision", "fp16"], ["--bins", "64x"], ["--bins", "64x64x"], ["--iterations"],
+             ["--iterations", "-3"], ["--iterations", "12abc"], ["--start", "left"], ["--target-density", "nan"],
+             ["--target-density", "abc"], ["--stop-overflow", "0.1x"], ["--device", "one"]]
+    for extra in usage:
+        r = subprocess.run(base + extra, capture_output=True, text=True, timeout=60)
+        assert r.returncode == 2, (extra, r.returncode, r.stderr)
+        assert "error" in r.stderr or "usage" in r.stderr, extra
+    r = subprocess.run([build.CLI, "-l", TECH, "-l", CELLS, "-d", str(tmp_path / "missing.def")],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "missing.def" in r.stderr
+    for extra, msg in ((["--bins", "30x16"], "powers of two"), (["--target-density", "0"], "target density"),
+                       (["--precision", "tf32", "--bins", "64x64"], "multiples of 128")):
+        r = subprocess.run(base + extra, capture_output=True, text=True, timeout=60)
+        assert r.returncode == 1 and msg in r.stderr, (extra, r.returncode, r.stderr)
