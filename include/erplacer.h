@@ -121,7 +121,8 @@ erp_status erp_create(const erp_design *design, const erp_params *params, erp_ct
 void erp_destroy(erp_ctx *ctx);
 
 /* compute_hpwl (src/hpwl.rs:139-343): WA wirelength gradient (kept on the
- * device) and the HPWL total (FP64 reduction).  hpwl may be NULL (no sync). */
+ * device) and the HPWL total (double-float reduction in a fixed order, returned as
+ * FP64).  hpwl may be NULL (no sync). */
 erp_status erp_wirelength(erp_ctx *ctx, float gamma, float *hpwl);
 
 /* compute_potential (src/epotential.rs:225-374): density scatter (int64 fixed
@@ -166,8 +167,8 @@ typedef struct erp_scalars {
     float alpha, beta;
     float hpwl_initial, hpwl_current, hpwl_previous;
     float overflow_current, overflow_previous;
-    double hpwl_last;         /* FP64 HPWL total of the last wirelength pass */
-    double overflow_last;     /* FP64 overflow of the last potential pass */
+    double hpwl_last;         /* HPWL total of the last wirelength pass (double-float sum) */
+    double overflow_last;     /* overflow of the last potential pass (double-float sum) */
     double energy_last;
     int32_t fixed_shift;      /* S: movable density contributions are rint(v * 2^S) */
     int32_t fixed_shift_init; /* S0 for the fixed-cell initial map */
