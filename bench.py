@@ -175,14 +175,15 @@ def make_workload(name):
     return d, cfg, desc
 
 
-def cpu_sample(d, cfg, iters, literal):
-    """Time `iters` oracle steps (all host threads) after one untimed step."""
+def cpu_sample(d, cfg, iters, literal, warmup=1):
+    """Time `iters` oracle steps (all host threads) after `warmup` untimed steps."""
     from oracle import erp_oracle as O
     m, n = cfg["bins"]
     o = O.Oracle(d, m, n, target_density=cfg["target_density"], start_mode=O.START_DB,
                  density_mode=O.DENSITY_REFERENCE if literal else O.DENSITY_FIXED,
                  reduce_fp64=0 if literal else 1, num_threads=0)
-    o.step()
+    for _ in range(max(1, warmup)):
+        o.step()
     t0 = time.perf_counter()
     for _ in range(iters):
         o.step()
@@ -515,18 +516,17 @@ def run_reference(args):
         return 0
     d, cfg, desc = make_workload(args.workload)
     iters = max(1, min(args.steps, args.ref_steps))
-    for _ in range(max(0, min(args.warmup, 1))):
-        pass
-    v, dt = cpu_sample(d, cfg, iters, literal=True)
+    warm = max(3, min(args.warmup, 10))   # untimed oracle iterations (about 0.2 s each at 1M cells)
+    v, dt = cpu_sample(d, cfg, iters, literal=True, warmup=warm)
     cores = os.cpu_count()
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
-        "steps": iters, "warmup": 1, "ms_per_step": 1000.0 * dt / iters,
+        "steps": iters, "warmup": warm, "ms_per_step": 1000.0 * dt / iters,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "config": {"workload": desc, "bins": list(cfg["bins"])},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{iters} full iterations of the workload after 1 untimed "
-                                   f"iteration; reference FP32 mode (sequential / atomic density)"},
+                         "sample": f"{iters} full iterations of the workload after {warm} untimed "
+                                   f"iterations; reference FP32 mode (sequential / atomic density)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
