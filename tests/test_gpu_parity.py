@@ -6,7 +6,10 @@ Bars (per stage, identical inputs on both sides):
     bit-exact;
   * WA pin/instance gradients, potential, fields, electric force: relative L2
     <= 1e-5 (FP32);
-  * HPWL / overflow totals: relative 1e-6 (FP64 reductions on both sides);
+  * HPWL / overflow totals: relative 1e-6 (double-float on the device, FP64 in
+    the oracle);
+  * scheduler: the same FP32 density weight and gamma as the oracle's FP64 form,
+    bit for bit;
   * end to end after the same iteration count: HPWL within 0.5 %, overflow
     within 0.005.
 """
@@ -96,6 +99,27 @@ def test_potential(case):
     assert abs(eg - eo) <= 1e-5 * abs(eo)
     assert rel_l2(g.array("DENS_GRAD_X"), o.get("dens_grad_x")) <= TOL
     assert rel_l2(g.array("DENS_GRAD_Y"), o.get("dens_grad_y")) <= TOL
+
+
+def test_scheduler_matches_the_fp64_form(R, O):
+    """erp_scheduler_update on the device against the oracle's FP64 form: both
+    evaluate b^e as exp(e ln b) in FP64 and cast to FP32, so a sequence of
+    updates through every branch (the density-weight growth and decay powers,
+    both clamps, the gamma coefficient and its clamps) gives the same bits."""
+    d = small_synth(3000, seed=12)
+    o, g = make_pair(R, O, d, 64, 64)
+    with g:
+        v, s = o.view(), g.scalars()
+        assert s["density_weight"] == v.density_weight and s["gamma"] == v.gamma
+        seq = [(1e6, 0.1), (5e5, 2.0), (6e5, 0.5), (4e5, 0.02), (4.5e5, 0.15), (3e5, 1.0)] + \
+              [(3e5 - 97.0 * k, 0.3 + 0.001 * k) for k in range(1, 250)]
+        for k, (hp, ov) in enumerate(seq):
+            o.scheduler_update(hp, ov)
+            g.scheduler_update(hp, ov)
+            v, s = o.view(), g.scalars()
+            assert s["iteration"] == v.iteration
+            assert s["density_weight"] == v.density_weight, k
+            assert s["gamma"] == v.gamma, k
 
 
 def test_nesterov_and_scheduler(case):

@@ -129,6 +129,37 @@ def test_scheduler_known_answers(O):
     assert not o.view().hpwl_initial_set == 0
 
 
+def test_scheduler_fp64_form_known_answers(O):
+    """The FP64 form (the device's): b^e of the constant bases as exp(e ln b),
+    the same clamps, then the FP32 casts; against math.pow, a sequence of
+    updates through every branch gives the same FP32 density weight and gamma."""
+    import math
+    d, _ = _wa_design()
+    o = O.Oracle(d, 16, 16, target_density=1.0, start_mode=O.START_DB, reduce_fp64=1)
+    v = o.view()
+    dw, base_gamma = float(v.density_weight), float(v.gamma)
+    f32 = lambda x: float(np.float32(x))
+    cur = 0.0
+    init = None
+    seq = [(100.0, 0.1), (50.0, 2.0), (60.0, 0.5), (40.0, 0.02), (45.0, 0.15), (30.0, 1.0)] + \
+          [(30.0 - 0.1 * k, 0.3) for k in range(1, 300)]
+    for it, (hp, ov) in enumerate(seq, start=1):
+        o.scheduler_update(hp, ov)
+        prev, cur = cur, f32(hp)
+        if init is None:
+            init = f32(hp)
+        delta = f32(cur - prev)
+        if delta < 0.0:
+            power = max(math.pow(0.9999, it), 0.98)
+        else:
+            power = min(max(math.pow(1.05, -delta / init), 0.95), 1.05)
+        dw = f32(dw * (1.05 * power))
+        coef = min(max(math.pow(10.0, (f32(ov) - 0.1) * 20.0 / 9.0 - 1.0), 0.05), 10.0)
+        v = o.view()
+        assert v.density_weight == dw, it
+        assert v.gamma == f32(base_gamma * coef), it
+
+
 def test_nesterov_momentum_and_clamp(O):
     d, _ = _wa_design()
     o = O.Oracle(d, 16, 16, target_density=1.0, start_mode=O.START_DB)
