@@ -1088,6 +1088,9 @@ extern "C" erp_status erp_restore(erp_ctx *ctx, const void *buf, size_t bytes) {
     if (bytes < ckpt_bytes(c)) { c.err = "truncated checkpoint"; return ERP_EINVAL; }
     const char *i = (const char *)buf + sizeof hd;
     memcpy(c.h_st, i, sizeof(DevState));
+    // between steps every reduction's arrival counter is zero; a damaged buffer
+    // must not leave the last-block finalizes of the next step unreachable
+    memset(c.h_st->ctr, 0, sizeof c.h_st->ctr);
     CK(cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream));
     i += sizeof(DevState);
     float *arr[kCkptArrays] = {c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy};
