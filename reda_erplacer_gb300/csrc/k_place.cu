@@ -593,8 +593,8 @@ __global__ void k_initial_density(int first, int count, const float *__restrict_
             const int bx = xl + k / ny, by = yl + k % ny;
             const float px = overlap_center(xi, sxi, bcx[bx], bw);
             const float py = overlap_center(yi, syi, bcy[by], bh);
-            const long long c = __float2ll_rn((px * py) * scale);
-            if (c) atomicAdd(acc + (size_t)bx * n + by, (unsigned long long)c);
+            const unsigned long long c = (unsigned long long)fxp_rint_u64((px * py) * scale);   // px, py >= 0
+            if (c) atomicAdd(acc + (size_t)bx * n + by, c);
         }
     }
 }
@@ -602,7 +602,7 @@ __global__ void k_initial_density(int first, int count, const float *__restrict_
 __global__ void k_initial_finalize(size_t mn, unsigned long long *__restrict__ acc, float inv,
                                    float td, float *__restrict__ initial) {
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < mn; k += (size_t)gridDim.x * blockDim.x) {
-        const float v = __ll2float_rn((long long)acc[k]) * inv;
+        const float v = fxp_u64_to_float(acc[k]) * inv;
         initial[k] = v * td;                                   // src/epotential.rs:138-140
         acc[k] = 0ull;
     }
