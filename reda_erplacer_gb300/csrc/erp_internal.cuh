@@ -17,8 +17,8 @@ constexpr int kThreads = 256;
 // Device-resident scalars.  Every quantity the reference keeps in Scheduler /
 // Nesterov (src/scheduler.rs:37-50, src/nesterov.rs:6-13) plus the reductions
 // of the current step, so that a whole Placement::step runs without a host
-// round trip (FP64 for the HPWL / overflow totals, the Lipschitz sums and the
-// density-weight update).
+// round trip (the HPWL / overflow totals and the Lipschitz sums are double-float
+// sums stored as FP64; the density-weight update is FP64).
 struct DevState {
     // scheduler
     int32_t iteration;
