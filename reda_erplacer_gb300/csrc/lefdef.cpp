@@ -57,6 +57,71 @@ struct Fail : std::runtime_error {
 // differences of a few of them never overflow int64.
 constexpr double kMaxUnits = 1099511627776.0;
 
+// Open-addressing table from names to the indices of their owners (macros,
+// macro pins, components, DEF pins).  It keeps only each key's hash and its
+// owner's index and compares against the owner's name, so the owners'
+// containers may reallocate.  insert keeps an existing entry (like emplace).
+class NameTable {
+  public:
+    template <class NameOf>
+    int find(std::string_view key, const NameOf &name_of) const {
+        if (count_ == 0) return -1;
+        const uint64_t h = hash(key);
+        for (size_t s = h & mask_;; s = (s + 1) & mask_) {
+            const int32_t i = idx_[s];
+            if (i < 0) return -1;
+            if (hash_[s] == h && name_of(i) == key) return i;
+        }
+    }
+    template <class NameOf>
+    bool insert(std::string_view key, int32_t owner, const NameOf &name_of) {
+        if ((count_ + 1) * 2 > idx_.size()) grow();
+        const uint64_t h = hash(key);
+        for (size_t s = h & mask_;; s = (s + 1) & mask_) {
+            const int32_t i = idx_[s];
+            if (i < 0) {
+                idx_[s] = owner;
+                hash_[s] = h;
+                ++count_;
+                return true;
+            }
+            if (hash_[s] == h && name_of(i) == key) return false;
+        }
+    }
+    bool empty() const { return count_ == 0; }
+
+  private:
+    static uint64_t hash(std::string_view k) {   // FNV-1a, then a 64-bit finaliser to spread the low bits
+        uint64_t h = 1469598103934665603ull;
+        for (unsigned char c : k) {
+            h ^= c;
+            h *= 1099511628211ull;
+        }
+        h ^= h >> 33;
+        h *= 0xff51afd7ed558ccdull;
+        h ^= h >> 33;
+        return h;
+    }
+    void grow() {
+        const size_t cap = idx_.empty() ? 64 : idx_.size() * 2;
+        std::vector<int32_t> idx(cap, -1);
+        std::vector<uint64_t> hs(cap, 0);
+        for (size_t s = 0; s < idx_.size(); ++s) {
+            if (idx_[s] < 0) continue;
+            size_t t = hash_[s] & (cap - 1);
+            while (idx[t] >= 0) t = (t + 1) & (cap - 1);
+            idx[t] = idx_[s];
+            hs[t] = hash_[s];
+        }
+        idx_.swap(idx);
+        hash_.swap(hs);
+        mask_ = cap - 1;
+    }
+    std::vector<int32_t> idx_;
+    std::vector<uint64_t> hash_;
+    size_t mask_ = 0, count_ = 0;
+};
+
 // llround(v) for a quantity in database units, or Fail.
 int64_t to_units(double v, const char *what) {
     if (!std::isfinite(v) || std::fabs(v) > kMaxUnits) throw Fail(std::string(what) + " out of range");
@@ -122,12 +187,13 @@ struct Macro {
     double w = 0, h = 0, ox = 0, oy = 0;      // microns
     int64_t W = 0, H = 0;                     // LEF grid units
     std::vector<MacroPin> pins;
-    std::unordered_map<std::string, int> index;   // built when there are many pins
-    int find_pin(const std::string &n) const {
-        if (!index.empty()) {
-            auto it = index.find(n);
-            return it == index.end() ? -1 : it->second;
-        }
+    NameTable index;   // built when there are many pins; the first of equal names wins
+    std::string_view pin_name(int k) const { return pins[k].name; }
+    void index_pin(int k) {
+        index.insert(pins[k].name, k, [this](int j) { return pin_name(j); });
+    }
+    int find_pin(std::string_view n) const {
+        if (!index.empty()) return index.find(n, [this](int j) { return pin_name(j); });
         for (size_t k = 0; k < pins.size(); ++k)
             if (pins[k].name == n) return (int)k;
         return -1;
@@ -161,7 +227,7 @@ struct erp_netlist {
     int64_t die[4] = {0, 0, 0, 0};
     bool have_die = false;
     std::vector<Macro> macros;
-    std::unordered_map<std::string, int> macro_index;
+    NameTable macro_index;
     int32_t num_components = 0;
     std::vector<Node> nodes;                   // parse order
     std::vector<std::string> net_names;        // kept nets, in DEF order
@@ -352,9 +418,9 @@ void lef_pin(Lex &L, Macro &m) {
     if (m.find_pin(pin.name) >= 0) L.fail("duplicate pin '" + pin.name + "' in macro '" + m.name + "'");
     m.pins.push_back(std::move(pin));
     if (m.pins.size() == 16) {
-        for (size_t k = 0; k < m.pins.size(); ++k) m.index.emplace(m.pins[k].name, (int)k);
+        for (size_t k = 0; k < m.pins.size(); ++k) m.index_pin((int)k);
     } else if (m.pins.size() > 16) {
-        m.index.emplace(m.pins.back().name, (int)m.pins.size() - 1);
+        m.index_pin((int)m.pins.size() - 1);
     }
 }
 
@@ -389,11 +455,12 @@ void lef_macro(Lex &L, erp_netlist &nl) {
             L.skip_statement();   // FOREIGN, SYMMETRY, SITE, PROPERTY, EEQ, SOURCE ...
         }
     }
-    auto it = nl.macro_index.find(m.name);
-    if (it != nl.macro_index.end()) {
-        nl.macros[it->second] = std::move(m);   // a later definition replaces an earlier one
+    auto macro_name = [&](int i) -> std::string_view { return nl.macros[i].name; };
+    const int prev = nl.macro_index.find(m.name, macro_name);
+    if (prev >= 0) {
+        nl.macros[prev] = std::move(m);   // a later definition replaces an earlier one
     } else {
-        nl.macro_index.emplace(m.name, (int)nl.macros.size());
+        nl.macro_index.insert(m.name, (int)nl.macros.size(), macro_name);
         nl.macros.push_back(std::move(m));
     }
 }
@@ -454,7 +521,7 @@ bool is_section(std::string_view k) {
 }
 
 struct DefState {
-    std::unordered_map<std::string, int> comp_index, pin_index;
+    NameTable comp_index, pin_index;   // component / DEF pin name -> node index
 };
 
 void def_components(Lex &L, erp_netlist &nl, DefState &S) {
@@ -466,10 +533,9 @@ void def_components(Lex &L, erp_netlist &nl, DefState &S) {
         if (L.t != "-") L.fail("expected '-' or 'END COMPONENTS', found '" + std::string(L.t) + "'");
         Node n;
         n.name = std::string(L.need());
-        const std::string master(L.need());
-        auto it = nl.macro_index.find(master);
-        if (it == nl.macro_index.end()) L.fail("component '" + n.name + "' of unknown macro '" + master + "'");
-        n.master = it->second;
+        const std::string_view master = L.need();
+        n.master = nl.macro_index.find(master, [&](int i) -> std::string_view { return nl.macros[i].name; });
+        if (n.master < 0) L.fail("component '" + n.name + "' of unknown macro '" + std::string(master) + "'");
         bool clause = false;
         for (;;) {
             L.need();
@@ -499,7 +565,8 @@ void def_components(Lex &L, erp_netlist &nl, DefState &S) {
             n.clause_off = L.off;   // the ';'
             n.clause_insert = true;
         }
-        if (!S.comp_index.emplace(n.name, (int)nl.nodes.size()).second) L.fail("duplicate component '" + n.name + "'");
+        if (!S.comp_index.insert(n.name, (int)nl.nodes.size(), [&](int i) -> std::string_view { return nl.nodes[i].name; }))
+            L.fail("duplicate component '" + n.name + "'");
         nl.nodes.push_back(std::move(n));
     }
     nl.num_components = (int32_t)nl.nodes.size();
@@ -556,7 +623,8 @@ void def_pins(Lex &L, erp_netlist &nl, DefState &S) {
             }
         }
         if (!n.placed) nl.st.num_unplaced_io++;
-        if (!S.pin_index.emplace(n.name, (int)nl.nodes.size()).second) L.fail("duplicate pin '" + n.name + "'");
+        if (!S.pin_index.insert(n.name, (int)nl.nodes.size(), [&](int i) -> std::string_view { return nl.nodes[i].name; }))
+            L.fail("duplicate pin '" + n.name + "'");
         nl.nodes.push_back(std::move(n));
     }
 }
@@ -564,7 +632,8 @@ void def_pins(Lex &L, erp_netlist &nl, DefState &S) {
 void def_nets(Lex &L, erp_netlist &nl, DefState &S) {
     L.need();
     L.expect(";");
-    std::string a, b;
+    auto node_name = [&](int i) -> std::string_view { return nl.nodes[i].name; };
+    std::string_view a, b;   // views into the DEF text, which outlives the parse
     for (;;) {
         L.need();
         if (L.t == "END") { L.expect("NETS"); break; }
@@ -582,24 +651,24 @@ void def_nets(Lex &L, erp_netlist &nl, DefState &S) {
             if (L.t == ";") break;
             if (L.t == "+") in_options = true;
             if (in_options || L.t != "(") continue;
-            a = std::string(L.need());
-            b = std::string(L.need());
+            a = L.need();
+            b = L.need();
             // "( comp pin + SYNTHESIZED )"
             do L.need();
             while (L.t != ")");
             if (a == "*") {
                 nl.st.num_skipped_conns++;
             } else if (a == "PIN") {
-                auto it = S.pin_index.find(b);
-                if (it == S.pin_index.end()) L.fail("net '" + name + "' names unknown pin '" + b + "'");
-                nl.conns.push_back({it->second, -1});
+                const int node = S.pin_index.find(b, node_name);
+                if (node < 0) L.fail("net '" + name + "' names unknown pin '" + std::string(b) + "'");
+                nl.conns.push_back({node, -1});
             } else {
-                auto it = S.comp_index.find(a);
-                if (it == S.comp_index.end()) L.fail("net '" + name + "' names unknown component '" + a + "'");
-                const Macro &m = nl.macros[nl.nodes[it->second].master];
+                const int node = S.comp_index.find(a, node_name);
+                if (node < 0) L.fail("net '" + name + "' names unknown component '" + std::string(a) + "'");
+                const Macro &m = nl.macros[nl.nodes[node].master];
                 const int k = m.find_pin(b);
-                if (k < 0) L.fail("net '" + name + "': macro '" + m.name + "' has no pin '" + b + "'");
-                nl.conns.push_back({it->second, k});
+                if (k < 0) L.fail("net '" + name + "': macro '" + m.name + "' has no pin '" + std::string(b) + "'");
+                nl.conns.push_back({node, k});
             }
         }
         if (nl.conns.size() == first) {
@@ -1106,9 +1175,10 @@ extern "C" erp_status erp_netlist_from_design(const erp_design *d, const erp_lef
                             m.pins.push_back(std::move(mp));
                         }
                         if (m.pins.size() >= 16)
-                            for (size_t k = 0; k < m.pins.size(); ++k) m.index.emplace(m.pins[k].name, (int)k);
+                            for (size_t k = 0; k < m.pins.size(); ++k) m.index_pin((int)k);
                         it = dedupe.emplace(key, (int)nl->macros.size()).first;
-                        nl->macro_index.emplace(m.name, (int)nl->macros.size());
+                        nl->macro_index.insert(m.name, (int)nl->macros.size(),
+                                               [&](int j) -> std::string_view { return nl->macros[j].name; });
                         nl->macros.push_back(std::move(m));
                     }
                     n.master = it->second;
