@@ -911,7 +911,58 @@ struct File {
 };
 
 // microns of n / den (exact decimal for the usual 100 .. 10000 grids)
+// n / den microns as "%.15g" prints the double n / den.  When den divides 10^6
+// (every DEF / LEF grid of 100 ... 10000 units per micron does), n / den is a
+// terminating decimal with at most six fraction digits; with at most 15
+// significant digits and a magnitude of at least 1e-4 (below 1e15 by the
+// bound on n), "%.15g" prints exactly that decimal with trailing zeros
+// removed, which is formed here in integers.  Anything else goes through
+// snprintf.
 std::string um(int64_t n, int64_t den) {
+    if (den > 0 && 1000000 % den == 0 && n > -100000000000000LL && n < 100000000000000LL) {
+        const uint64_t scale = (uint64_t)(1000000 / den);   // n / den = n * scale / 10^6
+        const bool neg = n < 0;
+        const uint64_t an = neg ? (uint64_t)(-n) : (uint64_t)n;
+        if (an <= UINT64_MAX / scale) {
+            const uint64_t q = an * scale;
+            if (q == 0) return "0";
+            const uint64_t ip = q / 1000000;
+            uint64_t fp = q % 1000000;
+            int frac = 6;   // fraction digits after removing trailing zeros
+            while (frac > 0 && fp % 10 == 0) {
+                fp /= 10;
+                --frac;
+            }
+            char idig[24];
+            int nd = 0;
+            for (uint64_t t = ip; t; t /= 10) idig[nd++] = (char)('0' + t % 10);
+            int sig;
+            if (ip > 0) {
+                sig = nd + frac;
+            } else {
+                int lead = 0;   // zeros between the point and the first nonzero digit
+                for (uint64_t t = q % 1000000; t < 100000; t *= 10) ++lead;
+                sig = frac - lead;
+                if (lead >= 4) sig = 99;   // below 1e-4: "%g" uses an exponent
+            }
+            if (sig <= 15) {
+                std::string out;
+                if (neg) out.push_back('-');
+                if (nd == 0) out.push_back('0');
+                while (nd) out.push_back(idig[--nd]);
+                if (frac > 0) {
+                    out.push_back('.');
+                    char fd[8];
+                    for (int k = frac - 1; k >= 0; --k) {
+                        fd[k] = (char)('0' + fp % 10);
+                        fp /= 10;
+                    }
+                    out.append(fd, (size_t)frac);
+                }
+                return out;
+            }
+        }
+    }
     char b[64];
     std::snprintf(b, sizeof b, "%.15g", (double)n / (double)den);
     return b;
