@@ -8,7 +8,9 @@ context's captured CUDA graph.  `value` is Nesterov iterations/s with the
 design resident in HBM; `e2e` is the same metric through the drop-in
 host-coordinate call erp_step_host (pinned host x/y copied in and out every
 step).  `--impl reference` times the CPU restatement of the reference loop
-(the oracle, reference FP32 mode) on the machine's host cores.
+(the oracle, reference FP32 mode) on the machine's host cores; that arm builds
+its input with the generator compiled on its own (oracle/_build/
+liberp_synth.so) and never loads the product library.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -46,9 +48,28 @@ ALG_BYTES = {
 }
 # DRAM bytes per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum)
 # of one --set full capture of the kernel on this workload (cold L2, the
-# profiler's default cache control); the command and figures are in
-# profiles/k_wa_1M_cells.md.
+# profiler's default cache control), taken with the command
+#   ncu --set full --clock-control none -k regex:k_wa -s 3 -c 1 -o k_wa \
+#       python bench.py --steps 20 --warmup 3 --no-cpu --batch-count 0 --quick
+# A bench run cannot count DRAM bytes itself, so the line labels this figure
+# as coming from that capture, not from the run.
 NCU_TRAFFIC = {("large", "wirelength"): 69.074176e6 + 15.063040e6}
+
+# The workloads: the synthetic generator's arguments and the run's
+# configuration.  The same data as reda_erplacer_gb300.design.WORKLOADS, kept
+# here so that the reference arm builds its input without importing the
+# package (tests/test_bench_fp64.py checks that the two agree).
+WORKLOADS = {
+    "small": (dict(num_cells=20000, num_nets=21000, num_io=400, num_macros=0, utilization=0.70, seed=1),
+              dict(bins=(256, 256), target_density=1.0, iterations=450)),
+    "large": (dict(num_cells=1000000, num_nets=1050000, num_io=4000, num_macros=16, macro_area_frac=0.015,
+                   utilization=0.65, seed=2),
+              dict(bins=(1024, 1024), target_density=1.0, iterations=1000)),
+}
+DESCS = {
+    "small": "plain FP32, 20,000 movable cells / 21,000 nets / 400 IO, 256x256 bins",
+    "large": "plain FP32, 1,000,000 movable cells / 1,050,000 nets / 16 macros / 4,000 IO, 1024x1024 bins",
+}
 
 
 def measured_peak_gbs():
@@ -164,32 +185,70 @@ def gather_items(items, world):
     return [x for part in out for x in part]
 
 
-def make_workload(name):
-    import reda_erplacer_gb300 as R
-    if name == "large":
-        d, cfg = R.workload_large()
-        desc = "plain FP32, 1,000,000 movable cells / 1,050,000 nets / 16 macros / 4,000 IO, 1024x1024 bins"
-    else:
-        d, cfg = R.workload_small()
-        desc = "plain FP32, 20,000 movable cells / 21,000 nets / 400 IO, 256x256 bins"
-    return d, cfg, desc
+def make_workload(name, generator):
+    """The named workload's design from `generator` (the package's synth, or the
+    oracle's copy of the same generator), its run configuration and label."""
+    args, cfg = WORKLOADS[name]
+    return generator(**args), dict(cfg), DESCS[name]
 
 
-def cpu_sample(d, cfg, iters, literal, warmup=1):
-    """Time `iters` oracle steps (all host threads) after `warmup` untimed steps."""
+def workload_config(d, cfg, desc):
+    """The line's `config`: the workload only, identical in both arms."""
+    m, n = cfg["bins"]
+    return {"workload": desc, "cells": int(d.num_movable), "nets": int(d.num_nets), "pins": int(d.num_pins),
+            "bins": [m, n], "target_density": cfg["target_density"], "iterations": cfg["iterations"],
+            "start": "die centre + Gaussian jitter (sigma 0.1% of die width)",
+            "parallelism": "replicas (one design per GPU)",
+            "l2": ("inputs larger than L2 (per-step working set > 129 MiB), no flush" if m * n >= 1 << 20
+                   else "working set smaller than L2, no flush (a step reuses the last step's data)")}
+
+
+def cpu_sample(d, cfg, iters, literal, warmup=1, trace=False):
+    """Time `iters` oracle steps (all host threads) after `warmup` untimed steps.
+    literal: the reference's own FP32 rules (sequential density below
+    iteration 200, then per-bin atomic adds; FP32 sums), else the fixed-point /
+    FP64 form.  trace: also return every step's (hpwl, overflow), warm-up
+    steps included, in iteration order."""
     from oracle import erp_oracle as O
     m, n = cfg["bins"]
     o = O.Oracle(d, m, n, target_density=cfg["target_density"], start_mode=O.START_DB,
                  density_mode=O.DENSITY_REFERENCE if literal else O.DENSITY_FIXED,
                  reduce_fp64=0 if literal else 1, num_threads=0)
+    hist = []
     for _ in range(max(1, warmup)):
-        o.step()
+        s = o.step()
+        hist.append((s["hpwl"], s["overflow"]))
     t0 = time.perf_counter()
     for _ in range(iters):
-        o.step()
+        s = o.step()
+        if trace:
+            hist.append((s["hpwl"], s["overflow"]))
     dt = time.perf_counter() - t0
     o.close()
-    return iters / dt, dt
+    return (iters / dt, dt, hist) if trace else (iters / dt, dt)
+
+
+def parity_summary(gpu, ref, tto_iteration):
+    """HPWL / overflow of the GPU run against the reference CPU loop, both from
+    the same start over the same iteration count: at the iteration where the
+    GPU run first reaches overflow 0.10, at each run's overflow minimum (the
+    converged state; past it the loop diverges and two summation orders of the
+    reference itself part), and at the last iteration."""
+    def at(k):
+        (hg, og), (hr, orf) = gpu[k], ref[k]
+        return {"iteration": k + 1, "hpwl_gpu": hg, "hpwl_ref": hr, "hpwl_rel": (hg - hr) / hr,
+                "overflow_gpu": og, "overflow_ref": orf, "overflow_abs": og - orf}
+    kg = min(range(len(gpu)), key=lambda k: gpu[k][1])
+    kr = min(range(len(ref)), key=lambda k: ref[k][1])
+    out = {"iterations": len(gpu), "last": at(len(gpu) - 1),
+           "overflow_min": {"iteration_gpu": kg + 1, "iteration_ref": kr + 1,
+                            "overflow_gpu": gpu[kg][1], "overflow_ref": ref[kr][1],
+                            "overflow_abs": gpu[kg][1] - ref[kr][1],
+                            "hpwl_gpu": gpu[kg][0], "hpwl_ref": ref[kr][0],
+                            "hpwl_rel": (gpu[kg][0] - ref[kr][0]) / ref[kr][0]}}
+    if tto_iteration:
+        out["at_overflow_0.10"] = at(tto_iteration - 1)
+    return out
 
 
 def batch_section(args, device, world=1, rank=0):
@@ -511,22 +570,28 @@ def serve_section(args, device, world=1, rank=0):
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference loop in its own
+    FP32 rules, on all host threads, on the same workload and config as the
+    GPU arm.  Its input comes from the generator compiled on its own
+    (oracle/_build/liberp_synth.so); the product library is never loaded."""
     world, rank, local = dist_setup()
     if rank != 0:
         return 0
-    d, cfg, desc = make_workload(args.workload)
-    iters = max(1, min(args.steps, args.ref_steps))
-    warm = max(3, min(args.warmup, 10))   # untimed oracle iterations (about 0.2 s each at 1M cells)
+    from oracle import erp_oracle as O
+    d, cfg, desc = make_workload(args.workload, O.synth)
+    iters = args.ref_steps if args.ref_steps > 0 else args.steps
+    warm = max(3, args.warmup)
     v, dt = cpu_sample(d, cfg, iters, literal=True, warmup=warm)
     cores = os.cpu_count()
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
         "steps": iters, "warmup": warm, "ms_per_step": 1000.0 * dt / iters,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": {"workload": desc, "bins": list(cfg["bins"])},
+        "data": "synthetic", "config": workload_config(d, cfg, desc),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{iters} full iterations of the workload after {warm} untimed "
-                                   f"iterations; reference FP32 mode (sequential / atomic density)"},
+                                   f"iterations, rank 0 only; oracle in the reference's FP32 rules "
+                                   f"(sequential density below iteration 200, then atomic adds)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -542,7 +607,7 @@ def run_ours(args):
     G.build_product()
     import reda_erplacer_gb300 as R
 
-    d, cfg, desc = make_workload(args.workload)
+    d, cfg, desc = make_workload(args.workload, R.synth)
     m, n = cfg["bins"]
     stream = torch.cuda.Stream()
     pl = R.Placement(d, (m, n), cfg["target_density"], start_mode=1, device=local,
@@ -625,26 +690,56 @@ def run_ours(args):
                "call": "erp_run(max_iterations, stop_overflow=0.10), context created beforehand"}
         pt.close()
 
+    # the workload's whole run (its configured iteration count) from a fresh
+    # context: the device-resident rate over every phase of the run (CUDA
+    # events, no per-step host sync), then the same run again with each step's
+    # HPWL and overflow read back, for the comparison with the reference loop
+    full = None
+    gpu_trace = []
+    if not args.no_full:
+        pf = R.Placement(d, (m, n), cfg["target_density"], start_mode=1, device=local,
+                         stream=stream.cuda_stream)
+        pf.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(cfg["iterations"]):
+            pf.step(stats=False)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fms = f0.elapsed_time(f1)
+        pf.close()
+        full = {"iterations": cfg["iterations"], "iters_per_s": cfg["iterations"] / (fms / 1000.0),
+                "ms_per_step": fms / cfg["iterations"],
+                "note": "fresh context, every iteration of the workload (spreading, converged and "
+                        "diverging phases); CUDA events on the context's stream"}
+        pg = R.Placement(d, (m, n), cfg["target_density"], start_mode=1, device=local)
+        for _ in range(cfg["iterations"]):
+            pg.step()
+            gpu_trace.append((pg.last_stats["hpwl"], pg.last_stats["overflow"]))
+        pg.close()
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": desc, "cells": d.num_movable, "nets": d.num_nets,
-                   "pins": d.num_pins, "bins": [m, n], "target_density": cfg["target_density"],
-                   "start": "die centre + Gaussian jitter (sigma 0.1% of die width)",
-                   "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (per-step working set > 129 MiB), no flush",
-                   "iteration_after": sc["iteration"], "hpwl_after": sc["hpwl_current"],
-                   "overflow_after": sc["overflow_current"]},
+        "config": workload_config(d, cfg, desc),
+        "timed_window": {"first_iteration": args.warmup, "iterations": args.steps,
+                         "iteration_after": sc["iteration"], "hpwl_after": sc["hpwl_current"],
+                         "overflow_after": sc["overflow_current"]},
         "clocks": clk,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps, "call": "erp_step_host"},
         "gpu_launches": int(st["graph_kernels"]) * args.steps,
         "roofline": {"kernel": "k_wa", "stage": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "alg_bytes": alg[dom], "ms": stages[dom]},
+                     "traffic": traffic,
+                     "traffic_source": "ncu capture of k_wa on this workload (dram read + write per "
+                                       "launch), not measured by this run",
+                     "alg_bytes": alg[dom], "ms": stages[dom]},
         "stages": per_stage,
         "time_to_overflow": tto,
+        "full_run": full,
     }
     if args.batch_count > 0:
         line["batched"] = batch_section(args, local, world, rank)
@@ -655,13 +750,63 @@ def run_ours(args):
     if args.serve_jobs > 0:
         line["serving"] = serve_section(args, local, world, rank)
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, dt = cpu_sample(d, cfg, args.cpu_iters, literal=False)
+        # the reference loop on the host cores: the oracle in the reference's own
+        # FP32 rules over the workload's whole run from the same start (one
+        # untimed first step); its trajectory is the CPU result the GPU run is
+        # compared with
+        iters = args.cpu_iters if args.cpu_iters > 0 else cfg["iterations"]
+        v, dt, ref_trace = cpu_sample(d, cfg, iters - 1, literal=True, warmup=1, trace=True)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"{args.cpu_iters} full iterations of the same workload "
-                                          f"(oracle, OpenMP, all host threads), {dt:.1f} s"}
+                                "sample": f"iterations 2-{iters} of the same workload from the same start "
+                                          f"(oracle in the reference's FP32 rules, OpenMP on all host "
+                                          f"threads), {dt:.1f} s"}
+        if gpu_trace and len(ref_trace) == len(gpu_trace):
+            line["parity_vs_reference"] = parity_summary(
+                gpu_trace, ref_trace, tto["iterations"] if tto and tto["reached"] else None)
     if rank == 0:
+        line["summary"] = summary(line)
         print(json.dumps(line), flush=True)
     return 0
+
+
+def summary(line):
+    """The headline figures of every section in a few short keys; printed last
+    in the line, so that a reader who sees only its tail still has them."""
+    out = {"iters_per_s": round(line["value"], 1), "e2e_iters_per_s": round(line["e2e"]["value"], 1)}
+    if line.get("full_run"):
+        out["full_run_iters_per_s"] = round(line["full_run"]["iters_per_s"], 1)
+    t = line.get("time_to_overflow")
+    if t:
+        out["time_to_overflow_0.10_s"] = round(t["seconds"], 4)
+        out["time_to_overflow_0.10_iterations"] = t["iterations"]
+    cb = line.get("cpu_baseline")
+    if cb:
+        out["cpu_reference_iters_per_s"] = round(cb["value"], 2)
+    pv = line.get("parity_vs_reference")
+    if pv:
+        k = pv.get("at_overflow_0.10", pv["last"])
+        out["parity_at_iteration"] = k["iteration"]
+        out["parity_hpwl_rel"] = round(k["hpwl_rel"], 5)
+        out["parity_overflow_abs"] = round(k["overflow_abs"], 5)
+        out["parity_min_overflow_abs"] = round(pv["overflow_min"]["overflow_abs"], 5)
+        out["parity_hpwl_rel_at_min_overflow"] = round(pv["overflow_min"]["hpwl_rel"], 5)
+    b = line.get("batched")
+    if b:
+        out["batched_jobs_per_hour"] = round(b["jobs_per_hour_batched"])
+        out["one_at_a_time_jobs_per_hour"] = round(b["jobs_per_hour_sequential"])
+        out["batched_speedup"] = round(b["speedup"], 3)
+        out["mixed_batched_speedup"] = round(b["mixed_batched"]["speedup_vs_fp32_one_at_a_time"], 3)
+    sv = line.get("serving")
+    if sv:
+        cb_ = sv["continuous_batching"]
+        out["serving_p50_s"] = round(cb_["p50_latency_s"], 3)
+        out["serving_p99_s"] = round(cb_["p99_latency_s"], 3)
+        out["serving_jobs_per_hour"] = round(cb_["jobs_per_hour"])
+        out["serving_retired_at_overflow"] = cb_["retired_at_overflow"]
+    sp = line.get("spectral_solve", {}).get("1024x1024")
+    if sp:
+        out["solve_1024_us"] = {k: round(v["us_per_solve"], 1) for k, v in sp.items()}
+    return out
 
 
 def main():
@@ -672,13 +817,16 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["large", "small"], default="large")
     ap.add_argument("--profile-reps", type=int, default=10)
-    ap.add_argument("--cpu-iters", type=int, default=3)
-    ap.add_argument("--ref-steps", type=int, default=10)
+    ap.add_argument("--cpu-iters", type=int, default=0,
+                    help="iterations of the CPU reference run beside the GPU arm (0: the workload's count)")
+    ap.add_argument("--ref-steps", type=int, default=0,
+                    help="timed iterations of the reference arm (0: the same as --steps)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true", help="timed steps only (for profiler runs)")
     ap.add_argument("--batch-count", type=int, default=64, help="instances of the batched section (0: skip)")
     ap.add_argument("--batch-iters", type=int, default=600)
     ap.add_argument("--no-tto", action="store_true", help="skip the time-to-overflow-0.10 run")
+    ap.add_argument("--no-full", action="store_true", help="skip the whole-run rate and trajectory")
     ap.add_argument("--no-spectral", action="store_true", help="skip the isolated-solve section")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision end-to-end runs")
     ap.add_argument("--spectral-reps", type=int, default=20)

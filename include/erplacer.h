@@ -10,7 +10,8 @@
  *
  * Each entry point names the reference function it replaces (file:line in the
  * reference crate).  The reference functions are `pub(crate)` Rust; the Rust
- * binding a maintainer adds (extern "C" block + build.rs) is in INTEGRATION.md.
+ * binding a maintainer adds is reda_erplacer_gb300/rust/ffi.rs (the extern "C"
+ * block and a safe Placement stand-in) with reda_erplacer_gb300/rust/build.rs.
  */
 #ifndef ERPLACER_H
 #define ERPLACER_H

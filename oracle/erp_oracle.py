@@ -4,15 +4,21 @@ Only tests/, __graft_entry__.smoke() and bench.py's CPU legs import this
 module, as the checker or the timed CPU baseline.  The product package never
 imports it.  Parity of the oracle against the reference binary is unpinned
 (see erp_oracle.h); it is pinned against FP64 closed forms in tests/golden.
+
+synth() builds the seeded synthetic netlists through liberp_synth.so, the
+package's generator source compiled on its own, so that a CPU leg can make its
+input design without loading the product library.
 """
 import ctypes as C
 import os
+from types import SimpleNamespace
 
 import numpy as np
 
 from . import build_oracle
 
 _lib = None
+_synth_lib = None
 
 f32p = C.POINTER(C.c_float)
 f64p = C.POINTER(C.c_double)
@@ -242,3 +248,57 @@ def poisson(rho, bin_w, bin_h, dtype=np.float32):
 
 def fixed_shift(total_area):
     return int(lib().erpo_fixed_shift(float(total_area)))
+
+
+class SynthParams(C.Structure):
+    """erp_synth_params of include/erplacer.h."""
+    _fields_ = [("seed", C.c_int64), ("num_cells", C.c_int32), ("num_nets", C.c_int32),
+                ("num_io", C.c_int32), ("num_macros", C.c_int32), ("macro_area_frac", C.c_float),
+                ("utilization", C.c_float), ("site_w", C.c_float), ("row_h", C.c_float),
+                ("min_sites", C.c_int32), ("max_sites", C.c_int32), ("jitter_frac", C.c_float)]
+
+
+def synth_lib():
+    global _synth_lib
+    if _synth_lib is None:
+        build_oracle.build_synth()
+        L = C.CDLL(build_oracle.SYNTH_LIB)
+        L.erp_synth_create.restype = C.c_int
+        L.erp_synth_create.argtypes = [C.POINTER(SynthParams), C.POINTER(C.c_void_p)]
+        L.erp_synth_design.restype = C.c_int
+        L.erp_synth_design.argtypes = [C.c_void_p, C.POINTER(Design)]
+        L.erp_synth_destroy.argtypes = [C.c_void_p]
+        _synth_lib = L
+    return _synth_lib
+
+
+def synth(num_cells, num_nets=None, num_io=0, num_macros=0, macro_area_frac=0.015, utilization=0.7,
+          seed=1, site_w=0.2, row_h=2.0, min_sites=2, max_sites=16, jitter_frac=0.001):
+    """The package's seeded synthetic netlist (same arguments as
+    reda_erplacer_gb300.synth, same bits), as a namespace of numpy arrays."""
+    L = synth_lib()
+    p = SynthParams(int(seed), int(num_cells), int(num_nets if num_nets else round(1.05 * num_cells)),
+                    int(num_io), int(num_macros), float(macro_area_frac), float(utilization),
+                    float(site_w), float(row_h), int(min_sites), int(max_sites), float(jitter_frac))
+    h = C.c_void_p()
+    st = L.erp_synth_create(C.byref(p), C.byref(h))
+    if st != 0:
+        raise ValueError(f"synthetic netlist: invalid parameters (status {st})")
+    try:
+        d = Design()
+        if L.erp_synth_design(h, C.byref(d)) != 0:
+            raise ValueError("synthetic netlist: no design")
+        N, P, E = d.num_nodes, d.num_pins, d.num_nets
+        net_ptr = _arr(d.net_ptr, E + 1, np.int32)
+        inst_ptr = _arr(d.inst_pin_ptr, N + 1, np.int32)
+        return SimpleNamespace(
+            num_nodes=N, num_movable=d.num_movable, num_pins=P, num_nets=E, n_2nets=d.n_2nets,
+            x=_arr(d.x, N), y=_arr(d.y, N), w=_arr(d.w, N), h=_arr(d.h, N),
+            num_pins_f=_arr(d.num_pins_f, N), pin_ox=_arr(d.pin_ox, P), pin_oy=_arr(d.pin_oy, P),
+            pin_inst=_arr(d.pin_inst, P, np.int32), net_ptr=net_ptr,
+            net_pins=_arr(d.net_pins, int(net_ptr[-1]), np.int32), inst_pin_ptr=inst_ptr,
+            inst_pins=_arr(d.inst_pins, int(inst_ptr[-1]), np.int32), die_w=float(d.die_w),
+            die_h=float(d.die_h), cell_utilization=float(d.cell_utilization),
+            movable_area=float(d.movable_area))
+    finally:
+        L.erp_synth_destroy(h)

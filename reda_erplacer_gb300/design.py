@@ -100,20 +100,40 @@ def synth(num_cells, num_nets=None, num_io=0, num_macros=0, macro_area_frac=0.01
         lib.erp_synth_destroy(h)
 
 
-# Workloads (seeded synthetic stand-ins for the reference's ISPD runs).
+# Workloads (seeded synthetic stand-ins for the reference's ISPD runs): the
+# generator's arguments and the run's configuration, as plain data so that a
+# CPU-only consumer can rebuild the same design with the generator alone.
+WORKLOADS = {
+    # 20,000 movable cells, 21,000 nets, 400 IO pins, 70 % utilisation; 256x256 bins,
+    # target density 1.0, 450 iterations
+    "small": (dict(num_cells=20000, num_nets=21000, num_io=400, num_macros=0, utilization=0.70, seed=1),
+              dict(bins=(256, 256), target_density=1.0, iterations=450)),
+    # 1,000,000 movable cells, 1,050,000 nets, 16 macros at 1.5 % of the die each, 4,000 IO
+    # pins, 65 % utilisation of the free area; 1024x1024 bins, 1,000 iterations
+    "large": (dict(num_cells=1000000, num_nets=1050000, num_io=4000, num_macros=16, macro_area_frac=0.015,
+                   utilization=0.65, seed=2),
+              dict(bins=(1024, 1024), target_density=1.0, iterations=1000)),
+}
+
+
+def workload(name, seed=None):
+    args, cfg = WORKLOADS[name]
+    args = dict(args)
+    if seed is not None:
+        args["seed"] = seed
+    return synth(**args), dict(cfg)
+
+
 def workload_small(seed=1):
     """20,000 movable cells, 21,000 nets, 400 IO pins, 70 % utilisation; 256x256 bins,
     target density 1.0, 450 iterations."""
-    return synth(20000, 21000, num_io=400, num_macros=0, utilization=0.70, seed=seed), \
-        dict(bins=(256, 256), target_density=1.0, iterations=450)
+    return workload("small", seed)
 
 
 def workload_large(seed=2):
     """1,000,000 movable cells, 1,050,000 nets, 16 macros at 1.5 % of the die each,
     4,000 IO pins, 65 % utilisation of the free area; 1024x1024 bins, 1,000 iterations."""
-    return synth(1000000, 1050000, num_io=4000, num_macros=16, macro_area_frac=0.015,
-                 utilization=0.65, seed=seed), \
-        dict(bins=(1024, 1024), target_density=1.0, iterations=1000)
+    return workload("large", seed)
 
 
 def batch_specs(count=64, seed=4000, min_cells=2000, max_cells=200000):

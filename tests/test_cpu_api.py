@@ -168,3 +168,37 @@ def test_design_struct_roundtrip(R):
     back = R.Design.from_struct(s)
     for k in ("x", "pin_inst", "net_ptr", "net_pins", "inst_pin_ptr", "inst_pins"):
         assert np.array_equal(getattr(back, k), getattr(d, k))
+
+
+def _c_struct_fields(txt, name):
+    """Field names of `typedef struct <name> { ... } <name>;` in declaration order."""
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), txt, flags=re.S).group(1)
+    out = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        decl = re.sub(r"\[[^\]]*\]", "", decl)
+        for part in decl.split(","):
+            out.append(re.findall(r"[A-Za-z_][A-Za-z0-9_]*", part)[-1])
+    return out
+
+
+def _rust_struct_fields(txt, name):
+    body = re.search(r"pub struct %s \{(.*?)\n\}" % name, txt, flags=re.S).group(1)
+    return re.findall(r"pub ([a-z_0-9]+):", body)
+
+
+def test_rust_binding_mirrors_the_header():
+    """reda_erplacer_gb300/rust/ffi.rs (the binding the reference crate would
+    add; no Rust toolchain here) declares every entry point of the header, and
+    its #[repr(C)] structs list the header's fields in the same order."""
+    h = open(os.path.join(ROOT, "include", "erplacer.h")).read()
+    h = re.sub(r"/\*.*?\*/", "", h, flags=re.S)
+    rs = open(os.path.join(ROOT, "reda_erplacer_gb300", "rust", "ffi.rs")).read()
+    decl = set(re.findall(r"pub fn (erp_[a-z0-9_]+)\s*\(", rs))
+    missing = [s for s in declared_symbols() if s not in decl]
+    assert not missing, missing
+    for st in ("erp_design", "erp_params", "erp_step_stats", "erp_scalars", "erp_server_params",
+               "erp_job_result", "erp_synth_params", "erp_lefdef_stats", "erp_lefdef_params"):
+        assert _c_struct_fields(h, st) == _rust_struct_fields(rs, st), st
