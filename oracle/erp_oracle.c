@@ -289,6 +289,14 @@ void erpo_set_scheduler(erpo_state *s, int32_t iteration, float gamma, float dw)
     s->iteration = iteration; s->gamma = gamma; s->dw = dw;
 }
 
+/* the scheduler's HpwlMetrics / OverflowMetrics (src/scheduler.rs:6-35) */
+void erpo_set_metrics(erpo_state *s, float hpwl_init, float hpwl_cur, float hpwl_prev, float ovf_cur,
+                      float ovf_prev) {
+    s->hpwl_init = hpwl_init; s->hpwl_cur = hpwl_cur; s->hpwl_prev = hpwl_prev;
+    s->ovf_cur = ovf_cur; s->ovf_prev = ovf_prev;
+    s->hpwl_init_set = 1; s->ovf_init_set = 1;
+}
+
 /* ---------------- wirelength: src/hpwl.rs ---------------- */
 
 /* one net, general path (src/hpwl.rs:248-334); the two-pin fast path

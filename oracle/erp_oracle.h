@@ -125,6 +125,9 @@ void erpo_set_positions(erpo_state *s, const float *x, const float *y);
 void erpo_set_nesterov_state(erpo_state *s, const float *px, const float *py,
                              const float *pgx, const float *pgy, float alpha, float beta);
 void erpo_set_scheduler(erpo_state *s, int32_t iteration, float gamma, float density_weight);
+/* HPWL / overflow metrics of the scheduler (initial, current, previous). */
+void erpo_set_metrics(erpo_state *s, float hpwl_init, float hpwl_cur, float hpwl_prev, float ovf_cur,
+                      float ovf_prev);
 
 /* src/hpwl.rs:139-343 */
 float erpo_compute_hpwl(erpo_state *s, float gamma);

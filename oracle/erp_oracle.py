@@ -82,6 +82,7 @@ def lib():
         L.erpo_set_positions.argtypes = [C.c_void_p, f32p, f32p]
         L.erpo_set_nesterov_state.argtypes = [C.c_void_p, f32p, f32p, f32p, f32p, C.c_float, C.c_float]
         L.erpo_set_scheduler.argtypes = [C.c_void_p, C.c_int32, C.c_float, C.c_float]
+        L.erpo_set_metrics.argtypes = [C.c_void_p] + [C.c_float] * 5
         L.erpo_compute_hpwl.restype = C.c_float
         L.erpo_compute_hpwl.argtypes = [C.c_void_p, C.c_float]
         L.erpo_compute_potential.restype = C.c_float
@@ -201,6 +202,23 @@ class Oracle:
 
     def set_scheduler(self, iteration, gamma, dw):
         self.L.erpo_set_scheduler(self.h, int(iteration), float(gamma), float(dw))
+
+    def set_metrics(self, hpwl_initial, hpwl_current, hpwl_previous, overflow_current, overflow_previous):
+        self.L.erpo_set_metrics(self.h, float(hpwl_initial), float(hpwl_current), float(hpwl_previous),
+                                float(overflow_current), float(overflow_previous))
+
+    def load_state(self, g):
+        """Copy a GPU placement's whole loop state (positions, Nesterov history,
+        scheduler and optimiser scalars) into the oracle, so that both continue
+        from the same state."""
+        x, y = g.positions()
+        self.set_positions(x, y)
+        s = g.scalars()
+        self.set_nesterov_state(g.array("PREV_X"), g.array("PREV_Y"), g.array("PREV_GX"),
+                                g.array("PREV_GY"), s["alpha"], s["beta"])
+        self.set_scheduler(s["iteration"], s["gamma"], s["density_weight"])
+        self.set_metrics(s["hpwl_initial"], s["hpwl_current"], s["hpwl_previous"], s["overflow_current"],
+                         s["overflow_previous"])
 
     def compute_hpwl(self, gamma):
         return float(self.L.erpo_compute_hpwl(self.h, float(gamma)))

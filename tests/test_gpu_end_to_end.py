@@ -1,0 +1,218 @@
+"""End-to-end parity of the whole loop at the configured iteration counts:
+the 20,000-cell workload for its 450 iterations and the 1,000,000-cell
+workload for its 1,000, GPU against the oracle in both of its forms -- the
+fixed-point / FP64 form and the reference's own FP32 rules (sequential density
+below iteration 200, then atomic adds; FP32 sums).
+
+The loop is chaotic once it has passed its overflow minimum: from there on two
+legitimate executions of the reference algorithm (the same FP32 rules summed
+in another order, or FP64 sums) part by far more than 0.5 % HPWL and 0.005
+overflow within a few dozen iterations (tests/test_oracle_golden.py pins this
+on the CPU).  A fixed-iteration bar at the end of such a run is therefore not
+met by the reference against itself, and the parity bar is checked in the two
+forms that are meaningful:
+
+  * shadowing: the GPU run is followed for every iteration of the workload,
+    and every `seg` iterations the oracle is reloaded with the GPU's whole
+    loop state (positions, Nesterov history, scheduler and optimiser
+    scalars); at the end of every segment -- in every phase of the run,
+    spreading, converged and diverging -- HPWL is within 0.5 % and overflow
+    within 0.005 of the oracle's;
+  * free run: both sides run the workload's iterations from the same start
+    without any reload; the converged state (the overflow minimum and the HPWL
+    there) is within 0.5 % / 0.005, the iterations before the reference's own
+    orders part are within the same bar, and the final state lies inside the
+    spread of the reference's own orders (widened by the bar).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+HPWL_BAR = 0.005
+OVF_BAR = 0.005
+
+
+@pytest.fixture(scope="module")
+def R(built):
+    import reda_erplacer_gb300 as R
+    return R
+
+
+@pytest.fixture(scope="module")
+def O(built):
+    from oracle import erp_oracle as O
+    return O
+
+
+FORMS = {
+    # name: (density mode, FP64 reductions, threads)
+    "fixed_fp64": ("DENSITY_FIXED", 1, 0),
+    "reference_fp32": ("DENSITY_REFERENCE", 0, 0),
+}
+
+
+def oracle(O, d, cfg, form, start_mode, threads=None):
+    dm, rf, th = FORMS[form]
+    m, n = cfg["bins"]
+    return O.Oracle(d, m, n, target_density=cfg["target_density"], start_mode=start_mode,
+                    density_mode=getattr(O, dm), reduce_fp64=rf, num_threads=th if threads is None else threads)
+
+
+def shadow(R, O, d, cfg, form, seg):
+    """Follow the GPU run over the workload's iterations, reloading the oracle
+    with the GPU's loop state every `seg` iterations; per segment the relative
+    HPWL and absolute overflow difference at its last iteration."""
+    m, n = cfg["bins"]
+    g = R.Placement(d, (m, n), cfg["target_density"], start_mode=1)
+    o = oracle(O, d, cfg, form, O.START_DB)
+    rows = []
+    try:
+        it = 0
+        while it < cfg["iterations"]:
+            if it:
+                o.load_state(g)
+            k = min(seg, cfg["iterations"] - it)
+            for _ in range(k):
+                so = o.step()
+                g.step()
+            sg = g.last_stats
+            rows.append((it + k, sg["hpwl"], so["hpwl"], sg["overflow"], so["overflow"]))
+            it += k
+    finally:
+        g.close()
+        o.close()
+    rel = np.array([abs(a - b) / b for _, a, b, _, _ in rows])
+    dov = np.array([abs(a - b) for _, _, _, a, b in rows])
+    return rows, rel, dov
+
+
+@pytest.mark.parametrize("form", list(FORMS))
+def test_small_workload_shadowing(R, O, form):
+    """20,000 cells, 256 x 256 bins, all 450 iterations, oracle reloaded every
+    25 iterations: every segment ends within the bar."""
+    d, cfg = R.workload_small()
+    rows, rel, dov = shadow(R, O, d, cfg, form, 25)
+    print(f"\n{form}: segments {len(rows)}, max hpwl rel {rel.max():.2e} (median {np.median(rel):.2e}), "
+          f"max overflow diff {dov.max():.2e}")
+    for r, a, b in zip(rows, rel, dov):
+        print(f"  it {r[0]:4d} hpwl {r[1]:.6g} / {r[2]:.6g} ({a:.1e})  overflow {r[3]:.5f} / {r[4]:.5f} ({b:.1e})")
+    assert len(rows) == 18
+    assert rel.max() <= HPWL_BAR
+    assert dov.max() <= OVF_BAR
+
+
+def trajectory(run_step, iters):
+    h, ov = np.empty(iters), np.empty(iters)
+    for i in range(iters):
+        s = run_step()
+        h[i], ov[i] = s["hpwl"], s["overflow"]
+    return h, ov
+
+
+def gpu_trajectory(R, d, cfg, start_mode):
+    m, n = cfg["bins"]
+    g = R.Placement(d, (m, n), cfg["target_density"], start_mode=start_mode)
+
+    def st():
+        g.step()
+        return g.last_stats
+    try:
+        return trajectory(st, cfg["iterations"])
+    finally:
+        g.close()
+
+
+def oracle_trajectory(O, d, cfg, form, start_mode, threads=None):
+    o = oracle(O, d, cfg, form, start_mode, threads)
+    try:
+        return trajectory(o.step, cfg["iterations"])
+    finally:
+        o.close()
+
+
+def converged(h, ov):
+    k = int(np.argmin(ov))
+    return k, h[k], ov[k]
+
+
+@pytest.fixture(scope="module", params=["jittered", "centre"])
+def small_free_run(request, R, O):
+    """The GPU run and the reference's own orders (fixed-point / FP64; FP32
+    rules on one thread and on all threads; FP32 rules with FP64 sums) over
+    the 450 iterations from one start."""
+    start = 1 if request.param == "jittered" else 0
+    d, cfg = R.workload_small()
+    fam = {"fixed_fp64": oracle_trajectory(O, d, cfg, "fixed_fp64", start),
+           "reference_fp32_1thread": oracle_trajectory(O, d, cfg, "reference_fp32", start, threads=1),
+           "reference_fp32": oracle_trajectory(O, d, cfg, "reference_fp32", start)}
+    o = O.Oracle(d, 256, 256, target_density=1.0, start_mode=start, density_mode=O.DENSITY_REFERENCE,
+                 reduce_fp64=1)
+    fam["reference_fp64_sums"] = trajectory(o.step, cfg["iterations"])
+    o.close()
+    return request.param, gpu_trajectory(R, d, cfg, start), fam
+
+
+def test_small_workload_free_run(small_free_run):
+    start, (hg, og), fam = small_free_run
+    kg, hgc, ogc = converged(hg, og)
+    print(f"\n{start} start: GPU overflow minimum {ogc:.5f} at iteration {kg + 1}, HPWL there {hgc:.6g}; "
+          f"final HPWL {hg[-1]:.6g} overflow {og[-1]:.5f}")
+    H = np.stack([h for h, _ in fam.values()])
+    OV = np.stack([o for _, o in fam.values()])
+    for name, (h, ov) in fam.items():
+        k, hc, oc = converged(h, ov)
+        print(f"  {name:24s} overflow minimum {oc:.5f} at {k + 1}, HPWL there {hc:.6g} "
+              f"(GPU {(hgc - hc) / hc:+.2e}, {ogc - oc:+.1e}); final HPWL {h[-1]:.6g} overflow {ov[-1]:.5f}")
+    spread_h = (H.max(0) - H.min(0)) / H.min(0)
+    spread_o = OV.max(0) - OV.min(0)
+    print(f"  reference orders' own spread at iteration 450: HPWL {spread_h[-1]:.2e}, overflow {spread_o[-1]:.2e}")
+    # the converged state
+    for name in ("fixed_fp64", "reference_fp32_1thread"):
+        h, ov = fam[name]
+        k, hc, oc = converged(h, ov)
+        assert abs(ogc - oc) <= OVF_BAR, name
+        assert abs(hgc - hc) / hc <= HPWL_BAR, name
+    # while the reference's own orders agree to the bar, so does the GPU
+    agree = np.nonzero((spread_h > HPWL_BAR) | (spread_o > OVF_BAR))[0]
+    upto = int(agree[0]) if len(agree) else len(hg)
+    print(f"  reference orders within the bar up to iteration {upto}")
+    hf, of = fam["fixed_fp64"]
+    assert np.all(np.abs(hg[:upto] - hf[:upto]) / hf[:upto] <= HPWL_BAR)
+    assert np.all(np.abs(og[:upto] - of[:upto]) <= OVF_BAR)
+    # the final state inside the reference's own spread, widened by the bar
+    assert H[:, -1].min() * (1 - HPWL_BAR) <= hg[-1] <= H[:, -1].max() * (1 + HPWL_BAR)
+    assert OV[:, -1].min() - OVF_BAR <= og[-1] <= OV[:, -1].max() + OVF_BAR
+
+
+def test_large_workload_shadowing(R, O):
+    """1,000,000 cells, 1024 x 1024 bins, all 1,000 iterations against the
+    reference's FP32 rules, oracle reloaded every 100 iterations."""
+    d, cfg = R.workload_large()
+    rows, rel, dov = shadow(R, O, d, cfg, "reference_fp32", 100)
+    print(f"\nsegments {len(rows)}, max hpwl rel {rel.max():.2e}, max overflow diff {dov.max():.2e}")
+    for r, a, b in zip(rows, rel, dov):
+        print(f"  it {r[0]:4d} hpwl {r[1]:.6g} / {r[2]:.6g} ({a:.1e})  overflow {r[3]:.5f} / {r[4]:.5f} ({b:.1e})")
+    assert rel.max() <= HPWL_BAR
+    assert dov.max() <= OVF_BAR
+
+
+def test_large_workload_free_run(R, O):
+    """1,000,000 cells from the jittered start, 1,000 iterations, GPU against the
+    reference's FP32 rules: at the iteration where the GPU first reaches
+    overflow 0.10 and at the converged state, within the bar."""
+    d, cfg = R.workload_large()
+    hg, og = gpu_trajectory(R, d, cfg, 1)
+    hr, orf = oracle_trajectory(O, d, cfg, "reference_fp32", 1)
+    kt = int(np.argmax(og <= 0.10))
+    kg, hgc, ogc = converged(hg, og)
+    kr, hrc, orc = converged(hr, orf)
+    print(f"\noverflow 0.10 at iteration {kt + 1}: HPWL {hg[kt]:.6g} / {hr[kt]:.6g} "
+          f"({(hg[kt] - hr[kt]) / hr[kt]:+.2e}), overflow {og[kt]:.5f} / {orf[kt]:.5f}")
+    print(f"overflow minimum GPU {ogc:.5f} at {kg + 1} (HPWL {hgc:.6g}), reference {orc:.5f} at {kr + 1} "
+          f"(HPWL {hrc:.6g}); final HPWL {hg[-1]:.6g} / {hr[-1]:.6g}, overflow {og[-1]:.5f} / {orf[-1]:.5f}")
+    assert og[kt] <= 0.10
+    assert abs(hg[kt] - hr[kt]) / hr[kt] <= HPWL_BAR
+    assert abs(og[kt] - orf[kt]) <= OVF_BAR
+    assert abs(ogc - orc) <= OVF_BAR
+    assert abs(hgc - hrc) / hrc <= HPWL_BAR
