@@ -91,8 +91,17 @@ typedef struct erp_params {
     int32_t precision;        /* erp_precision */
     int32_t device;           /* CUDA device ordinal */
     void *stream;             /* cudaStream_t to run on; NULL: the context creates its own */
-    int32_t flags;            /* reserved, 0 */
+    int32_t flags;            /* 0, or ERP_FLAG_EXPIRE_WAITS */
 } erp_params;
+
+/* Test hook of the bounded device waits.  Every kernel wait on a bulk copy
+ * into shared memory gives up at once instead of after its limit; the kernel
+ * then drains the copy with the full limit, records the timeout and retires
+ * the context, exactly as when a copy really stalls, and the call returns
+ * ERP_ETIMEDOUT.  Nothing on the device is left waiting or in flight.  Only
+ * the FP32 spectral path's row pass waits on copies, at bin counts of 64 and
+ * more in the row direction; other contexts ignore the flag. */
+#define ERP_FLAG_EXPIRE_WAITS 1
 
 /* One Placement::step's scalars (the reference logs these every 10
  * iterations, src/placement.rs:213-223).  gamma and density_weight are the
@@ -353,8 +362,12 @@ void erp_spectral_destroy(erp_spectral *sp);
  * rejected with ERP_EINVAL.  The caller passes device buffers of m*n floats
  * (potential may be NULL) and a stream (NULL: the legacy default stream).
  * The first call on a device looks up the array's address and sets kernel
- * limits: make it before any stream capture.  Every call reuses the array, so
- * calls that overlap on the GPU race; sequential calls are independent. */
+ * limits: make it before any stream capture.  That address is kept for the
+ * life of the process: cudaDeviceReset after the first call is not supported.
+ * Every call reuses the array, so calls that overlap on the GPU race;
+ * sequential calls are independent.  Results agree with erp_spectral_solve
+ * within FP32 rounding (its twiddle tables are built on the device), not bit
+ * for bit. */
 #define ERP_NOALLOC_MAX_BINS (512 * 512)
 erp_status erp_spectral_solve_noalloc(int32_t m, int32_t n, float bin_w, float bin_h,
                                       const float *rho_dev, float *field_x_dev,

@@ -50,9 +50,9 @@ __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
 }
 
 // Wait for the barrier phase with the given parity to complete; false once
-// kWaitTries tries have run out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitTries; ++i)
+// `tries` tries (kWaitTries unless given) have run out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t tries = kWaitTries) {
+    for (uint32_t i = 0; i < tries; ++i)
         if (mbar_try(bar, parity)) return true;
     return false;
 }

@@ -242,6 +242,11 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
         c.err = "unsupported precision";
         return ERP_ENOTSUP;
     }
+    if (prm.flags & ~ERP_FLAG_EXPIRE_WAITS) {
+        c.err = "unknown flags";
+        return ERP_EINVAL;
+    }
+    c.expire_waits = (prm.flags & ERP_FLAG_EXPIRE_WAITS) ? 1u : 0u;
     if (prm.precision != ERP_PREC_FP32 && (prm.num_bins_x % 128 || prm.num_bins_y % 128)) {
         c.err = "the tensor-core spectral solve needs bin counts that are multiples of 128";
         return ERP_EINVAL;
@@ -310,6 +315,19 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     c.shift0 = fixed_shift(fix_tot);
     c.fixed_scale = ldexpf(1.0f, c.shift);
     c.fixed_inv = ldexpf(1.0f, -c.shift);
+    {
+        // The scatter keeps each contribution rint((px * py) * 2^S) in 21-bit
+        // pieces; two pieces suffice when no contribution reaches 2^42.  A
+        // contribution is at most ratio * x-overlap * y-overlap * 2^S, an overlap
+        // at most the bin size plus the rounding of a bin edge (a few ulps of the
+        // die), the ratio of a movable cell at most 1 (checked here).
+        double rmax = 0;
+        for (int i = 0; i < NM; ++i) rmax = std::max(rmax, (double)hr[i]);
+        const double ex = ldexp((double)d->die_w + c.bin_w, -20), ey = ldexp((double)d->die_h + c.bin_h, -20);
+        const double cmax = std::max(rmax, 1.0) * ((double)c.bin_w + ex) * ((double)c.bin_h + ey) *
+                            ldexp(1.0, c.shift) * (1.0 + ldexp(1.0, -16));
+        c.scatter_planes = cmax < ldexp(1.0, 42) ? 2 : 3;
+    }
     // --- nets: degree classes, internal order, pin slots ---
     std::vector<int> cls_of(E);
     int counts[kNumClasses] = {0};
@@ -445,6 +463,7 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     h.dw = 8e-5f;
     h.alpha = 1.0f;
     h.beta = 0.0f;
+    h.expire_waits = c.expire_waits;
     *c.h_st = h;
     CK(cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream));
     launch_pack_xy(c);
@@ -1091,6 +1110,7 @@ extern "C" erp_status erp_restore(erp_ctx *ctx, const void *buf, size_t bytes) {
     // between steps every reduction's arrival counter is zero; a damaged buffer
     // must not leave the last-block finalizes of the next step unreachable
     memset(c.h_st->ctr, 0, sizeof c.h_st->ctr);
+    c.h_st->expire_waits = c.expire_waits;   // the restoring context's own wait rule
     CK(cudaMemcpyAsync(c.st, c.h_st, sizeof(DevState), cudaMemcpyHostToDevice, c.stream));
     i += sizeof(DevState);
     float *arr[kCkptArrays] = {c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy};

@@ -43,6 +43,10 @@ struct DevState {
     int32_t stop_iter;     // > 0: retire once iteration reaches it
     int32_t last_iter;     // iteration index of the last completed step
     erp_step_stats last;   // stats of the last completed step
+    // 1 under ERP_FLAG_EXPIRE_WAITS: a kernel's mbarrier wait gives up at once
+    // instead of after kWaitTries tries (the copy is then still drained with
+    // the full limit before the shared area is reused); 0 otherwise
+    uint32_t expire_waits;
     // last-block counters of the deterministic reductions
     uint32_t ctr[8];
 };
@@ -81,6 +85,7 @@ struct Ctx {
     int device;
     cudaStream_t stream;
     bool own_stream;
+    uint32_t expire_waits;   // DevState::expire_waits of this context
     std::string err;
     // --- cells [N] ---
     float *x, *y, *w, *h, *npins, *cw, *ch, *offx, *offy, *ratio;
@@ -103,6 +108,7 @@ struct Ctx {
     int32_t *sort_key, *sort_rank, *sort_hist, *sort_start;   // counting-sort scratch ([NM], [NM], tiles, tiles)
     int32_t sort_age;          // steps since the order was computed
     int32_t scatter_cells;     // movable cells per scatter block; 0: the rule for a context run alone
+    int32_t scatter_planes;    // 21-bit pieces per contribution in the scatter's window: 2 or 3
     // host-side permutations for test hooks
     int32_t *h_slot_of_pin;    // [P]
     int32_t *h_net_of_internal;// [E]

@@ -20,6 +20,12 @@
 //  * the first call on a device does that device's set-up (it looks up the
 //    array's device address with cudaGetSymbolAddress and sets the kernels'
 //    shared-memory limits); make that first call before any stream capture.
+//    The address is kept for the life of the process, so cudaDeviceReset on a
+//    device after its first call is not supported (the reset rebuilds the
+//    module and moves the array);
+//  * the twiddle tables are built on the device here, and on the host for
+//    erp_spectral_solve, so the two solves agree within FP32 rounding (the
+//    tests' 1e-5 relative L2), not bit for bit.
 #include <math.h>
 
 #include <mutex>

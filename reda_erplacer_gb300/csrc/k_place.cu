@@ -365,15 +365,75 @@ constexpr int kTableLog = 9, kTable = 1 << kTableLog;   // out-of-window bin tab
 constexpr unsigned kEmpty = 0xffffffffu;                 // bin indices are < 4096 * 4096
 constexpr int kMaxCellsPerBlock = 2048;
 constexpr unsigned long long kPiece = (1ull << 21) - 1;
+// The contribution c = rint((px * py) * 2^S) of one (cell, bin) pair to the
+// block's window, its bin table, or global memory, as PLANES 21-bit pieces.
+template <int PLANES>
+__device__ __forceinline__ void scatter_add(int bx, int by, unsigned long long c, int wox, int woy, int n,
+                                            unsigned *win, unsigned *tkey, unsigned *tplane,
+                                            unsigned long long *__restrict__ map) {
+    const unsigned wx = (unsigned)(bx - wox), wy = (unsigned)(by - woy);
+    if (wx < (unsigned)kWin && wy < (unsigned)kWin) {
+        unsigned *w = win + wx * kWin + wy;
+        atomicAdd(w, (unsigned)(c & kPiece));
+        if (c >> 21) {
+            atomicAdd(w + kWin * kWin, (unsigned)((c >> 21) & kPiece));
+            if (PLANES == 3 && (c >> 42)) atomicAdd(w + 2 * kWin * kWin, (unsigned)(c >> 42));
+        }
+        return;
+    }
+    // outside the window: the block's bin table, else global memory
+    const unsigned bin = (unsigned)bx * (unsigned)n + (unsigned)by;
+    const unsigned slot = (bin * 2654435761u) >> (32 - kTableLog);
+    unsigned k = tkey[slot];
+    if (k == kEmpty) {
+        k = atomicCAS(tkey + slot, kEmpty, bin);
+        if (k == kEmpty) k = bin;
+    }
+    if (k == bin) {
+        unsigned *t = tplane + slot;
+        atomicAdd(t, (unsigned)(c & kPiece));
+        if (c >> 21) {
+            atomicAdd(t + kTable, (unsigned)((c >> 21) & kPiece));
+            if (PLANES == 3 && (c >> 42)) atomicAdd(t + 2 * kTable, (unsigned)(c >> 42));
+        }
+    } else {
+        atomicAdd(map + bin, c);
+    }
+}
+
+// Overlaps of one cell with up to four consecutive bins starting at k0 (zero
+// beyond `count`), shifted so that the first nonzero one comes first; returns
+// the length of the run up to the last nonzero overlap and advances k0 past the
+// leading zeros.  Zeros inside the run only give zero contributions, which add
+// nothing to an integer sum.
+__device__ __forceinline__ int overlap_run4(float x, float s, int &k0, int count, float bs, float mul,
+                                            float (&t)[4]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) t[j] = j < count ? mul * tri_clamped(x, s, k0 + j, bs) : 0.0f;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        if (t[0] == 0.0f) {
+            t[0] = t[1]; t[1] = t[2]; t[2] = t[3]; t[3] = 0.0f;
+            ++k0;
+        }
+    }
+    return t[3] != 0.0f ? 4 : t[2] != 0.0f ? 3 : t[1] != 0.0f ? 2 : t[0] != 0.0f ? 1 : 0;
+}
+
+__device__ __forceinline__ float pick4(const float (&t)[4], int j) {
+    return j == 0 ? t[0] : j == 1 ? t[1] : j == 2 ? t[2] : t[3];
+}
+
+template <int PLANES>
 __global__ void __launch_bounds__(kThreads) k_density_scatter(
     int NM, const int32_t *__restrict__ perm, const float2 *__restrict__ xy, const float4 *__restrict__ soff,
     const float *__restrict__ sratio, const int32_t *__restrict__ skey, int nty, int m, int n, float bw,
     float bh, float inv_bw, float inv_bh, float scale, unsigned long long *__restrict__ map,
     const DevState *__restrict__ st) {
     extern __shared__ unsigned dsm[];
-    unsigned *win = dsm;                            // window planes: bits 0-20, 21-41, 42-62
-    unsigned *tkey = dsm + 3 * kWin * kWin;          // bin table: keys (bin index or kEmpty)
-    unsigned *tplane = tkey + kTable;                // bin table: planes
+    unsigned *win = dsm;                                  // window planes: bits 0-20, 21-41 (, 42-62)
+    unsigned *tkey = dsm + PLANES * kWin * kWin;          // bin table: keys (bin index or kEmpty)
+    unsigned *tplane = tkey + kTable;                     // bin table: planes
     if (st->done) return;
     const int per = ((NM + gridDim.x - 1) / gridDim.x + 31) & ~31;   // <= kMaxCellsPerBlock (launcher)
     const int c0 = blockIdx.x * per, c1 = min(c0 + per, NM);
@@ -385,9 +445,12 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
     }
     wox = max(0, min(wox, m - kWin));
     woy = max(0, min(woy, n - kWin));
-    for (int k = threadIdx.x; k < 3 * kWin * kWin; k += blockDim.x) win[k] = 0u;
-    for (int k = threadIdx.x; k < kTable; k += blockDim.x) tkey[k] = kEmpty;
-    for (int k = threadIdx.x; k < 3 * kTable; k += blockDim.x) tplane[k] = 0u;
+    {
+        uint4 *w4 = reinterpret_cast<uint4 *>(dsm);
+        for (int k = threadIdx.x; k < PLANES * kWin * kWin / 4; k += blockDim.x) w4[k] = make_uint4(0u, 0u, 0u, 0u);
+        for (int k = threadIdx.x; k < kTable; k += blockDim.x) tkey[k] = kEmpty;
+        for (int k = threadIdx.x; k < PLANES * kTable; k += blockDim.x) tplane[k] = 0u;
+    }
     __syncthreads();
     for (int base = c0; base < c1; base += blockDim.x) {
         const int p = base + threadIdx.x;
@@ -411,64 +474,56 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
             nx = max(xh - xl, 0);
             ny = max(yh - yl, 0);
         }
-        auto add = [&](int bx, int by, unsigned long long c) {
-            const int wx = bx - wox, wy = by - woy;
-            if (wx >= 0 && wx < kWin && wy >= 0 && wy < kWin) {
-                unsigned *w = win + wx * kWin + wy;
-                atomicAdd(w, (unsigned)(c & kPiece));
-                if (c >> 21) {
-                    atomicAdd(w + kWin * kWin, (unsigned)((c >> 21) & kPiece));
-                    if (c >> 42) atomicAdd(w + 2 * kWin * kWin, (unsigned)(c >> 42));
-                }
-            } else {   // outside the window: the block's bin table, else global memory
-                const unsigned bin = (unsigned)bx * (unsigned)n + (unsigned)by;
-                const unsigned slot = (bin * 2654435761u) >> (32 - kTableLog);
-                unsigned k = tkey[slot];
-                if (k == kEmpty) {
-                    k = atomicCAS(tkey + slot, kEmpty, bin);
-                    if (k == kEmpty) k = bin;
-                }
-                if (k == bin) {
-                    unsigned *t = tplane + slot;
-                    atomicAdd(t, (unsigned)(c & kPiece));
-                    if (c >> 21) {
-                        atomicAdd(t + kTable, (unsigned)((c >> 21) & kPiece));
-                        if (c >> 42) atomicAdd(t + 2 * kTable, (unsigned)(c >> 42));
-                    }
-                } else {
-                    atomicAdd(map + bin, c);
+        if (nx <= 4 && ny <= 4) {
+            // standard cells: every overlap computed once, the cell's (x, y) pairs
+            // walked in one flat loop (px = r * x-overlap, py = y-overlap; the
+            // contribution rint((px * py) * 2^S) as in the oracle)
+            float tx[4], ty[4];
+            const int cx = overlap_run4(xi, sxi, bxl, nx, bw, r, tx);
+            const int cy = overlap_run4(yi, syi, byl, ny, bh, 1.0f, ty);
+            const int cnt = cx * cy;
+            int dx = 0, dy = 0;
+            for (int k = 0; k < cnt; ++k) {
+                const float px = pick4(tx, dx), py = pick4(ty, dy);
+                const unsigned long long c = (unsigned long long)fxp_rint_u64((px * py) * scale);
+                if (c) scatter_add<PLANES>(bxl + dx, byl + dy, c, wox, woy, n, win, tkey, tplane, map);
+                if (++dy == cy) {
+                    dy = 0;
+                    ++dx;
                 }
             }
-        };
-        for (int dx = 0; dx < nx; ++dx) {
-            const int bx = bxl + dx;
-            const float px = r * tri_clamped(xi, sxi, bx, bw);
-            if (px == 0.0f) continue;   // every contribution of this bin column is 0
-            for (int dy = 0; dy < ny; ++dy) {
-                const int by = byl + dy;
-                const float py = tri_clamped(yi, syi, by, bh);
-                const unsigned long long c = (unsigned long long)fxp_rint_u64((px * py) * scale);
-                if (c) add(bx, by, c);
+        } else {
+            // larger cells: the bin columns and rows in full
+            for (int dx = 0; dx < nx; ++dx) {
+                const int bx = bxl + dx;
+                const float px = r * tri_clamped(xi, sxi, bx, bw);
+                if (px == 0.0f) continue;   // every contribution of this bin column is 0
+                for (int dy = 0; dy < ny; ++dy) {
+                    const int by = byl + dy;
+                    const float py = tri_clamped(yi, syi, by, bh);
+                    const unsigned long long c = (unsigned long long)fxp_rint_u64((px * py) * scale);
+                    if (c) scatter_add<PLANES>(bx, by, c, wox, woy, n, win, tkey, tplane, map);
+                }
             }
         }
     }
     __syncthreads();
     for (int k = threadIdx.x; k < kWin * kWin; k += blockDim.x) {
-        const unsigned long long v = (unsigned long long)win[k] + ((unsigned long long)win[k + kWin * kWin] << 21) +
-                                     ((unsigned long long)win[k + 2 * kWin * kWin] << 42);
+        unsigned long long v = (unsigned long long)win[k] + ((unsigned long long)win[k + kWin * kWin] << 21);
+        if (PLANES == 3) v += (unsigned long long)win[k + 2 * kWin * kWin] << 42;
         const int bx = wox + k / kWin, by = woy + k % kWin;
         if (v && bx < m && by < n) atomicAdd(map + (size_t)bx * n + by, v);
     }
     for (int k = threadIdx.x; k < kTable; k += blockDim.x) {
         const unsigned bin = tkey[k];
         if (bin == kEmpty) continue;
-        const unsigned long long v = (unsigned long long)tplane[k] + ((unsigned long long)tplane[k + kTable] << 21) +
-                                     ((unsigned long long)tplane[k + 2 * kTable] << 42);
+        unsigned long long v = (unsigned long long)tplane[k] + ((unsigned long long)tplane[k + kTable] << 21);
+        if (PLANES == 3) v += (unsigned long long)tplane[k + 2 * kTable] << 42;
         if (v) atomicAdd(map + bin, v);
     }
 }
 
-size_t density_scatter_smem() { return sizeof(unsigned) * (3 * kWin * kWin + 4 * kTable); }
+size_t density_scatter_smem(int planes) { return sizeof(unsigned) * (planes * kWin * kWin + (planes + 1) * kTable); }
 
 // Scatter order: counting sort of the movable cells by sort tile.  Ranks within
 // a tile follow atomic order (any order is valid, see k_density_scatter).
@@ -560,8 +615,11 @@ __global__ void __launch_bounds__(kThreads) k_sort_place(int NM, const int32_t *
 int scatter_tiles(int m, int n) { return ((m + kSortTile - 1) / kSortTile) * ((n + kSortTile - 1) / kSortTile); }
 
 cudaError_t place_prepare() {
-    return cudaFuncSetAttribute(k_density_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)density_scatter_smem());
+    cudaError_t e = cudaFuncSetAttribute(k_density_scatter<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)density_scatter_smem(2));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_density_scatter<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)density_scatter_smem(3));
 }
 
 // compute_density_overflow (src/density.rs:16-23): overlap through bin centres
@@ -1060,7 +1118,8 @@ void launch_density_scatter(Ctx &c) {
     const int g = c.scatter_cells > 0 ? std::max((c.NM + c.scatter_cells - 1) / c.scatter_cells, std::max(floor_g, 1))
                                       : std::max(grid_for(c.NM, 152 * 4), floor_g);
     const int nty = (c.n + kSortTile - 1) / kSortTile;
-    k_density_scatter<<<g, kThreads, density_scatter_smem(), c.stream>>>(
+    auto kern = c.scatter_planes == 2 ? k_density_scatter<2> : k_density_scatter<3>;
+    kern<<<g, kThreads, density_scatter_smem(c.scatter_planes), c.stream>>>(
         c.NM, c.perm, c.xy, c.soff, c.sratio, c.skey, nty, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw,
         c.inv_bh, c.fixed_scale, c.dmap, c.st);
 }

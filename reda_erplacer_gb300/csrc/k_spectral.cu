@@ -507,7 +507,7 @@ __global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
     const AxisTables tb = load_tables<NW, H>(sm, tw_n, ek_n);
     Df ovf = df_zero();
     if (from_map) {
-        if (!mbar_wait(&bar[warp], 0)) {
+        if (!mbar_wait(&bar[warp], 0, (st && st->expire_waits) ? 0u : kWaitTries)) {
             if (lane == 0 && st) {
                 atomicOr(&st->status, kStatusWaitTimeout);
                 st->done = 1;
@@ -841,7 +841,7 @@ __global__ void __launch_bounds__(G * kQ * 32) k_rows_dct_g(
     Df ovf = df_zero();
     float v[PT];
     if (from_map) {
-        if (!mbar_wait(&bar[grp], 0)) {
+        if (!mbar_wait(&bar[grp], 0, (st && st->expire_waits) ? 0u : kWaitTries)) {
             if (gt == 0 && st) {
                 atomicOr(&st->status, kStatusWaitTimeout);
                 st->done = 1;

@@ -19,6 +19,7 @@ OK, EINVAL, ENOMEM, ECUDA, ENAN, ETIMEDOUT, ENOTSUP, ENODEV, ESTATE = range(9)
 START_CENTER, START_DB = 0, 1
 STAGES = ("wirelength", "wl_gather", "density", "spectral", "force", "nesterov", "scheduler")
 PREC_FP32, PREC_TF32_GEMM, PREC_BF16X3_GEMM = 0, 1, 2
+FLAG_EXPIRE_WAITS = 1   # erp_params.flags: test hook of the bounded device waits
 
 ARR = dict(WL_GRAD_X=0, WL_GRAD_Y=1, DENS_GRAD_X=2, DENS_GRAD_Y=3, PIN_GRAD_X=4, PIN_GRAD_Y=5,
            DENSITY_I64=6, DENSITY=7, INITIAL=8, FIELD_X=9, FIELD_Y=10, POTENTIAL=11, PREV_X=12,

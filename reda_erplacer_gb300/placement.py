@@ -28,13 +28,14 @@ def write_ppm(path, img):
 
 class Placement:
     def __init__(self, design, num_bins=(512, 512), target_density=-1.0,
-                 start_mode=L.START_CENTER, device=0, stream=None, precision=L.PREC_FP32):
+                 start_mode=L.START_CENTER, device=0, stream=None, precision=L.PREC_FP32, flags=0):
         self.lib = L.load()
         self.design = design
         self._ds = design.to_struct()
         m, n = num_bins
         self._params = L.Params(int(m), int(n), float(target_density), int(start_mode),
-                                int(precision), int(device), C.c_void_p(stream) if stream else None, 0)
+                                int(precision), int(device), C.c_void_p(stream) if stream else None,
+                                int(flags))
         h = C.c_void_p()
         st = self.lib.erp_create(C.byref(self._ds), C.byref(self._params), C.byref(h))
         L.check(st, None)

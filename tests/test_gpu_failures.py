@@ -12,6 +12,11 @@
   rejects, a non-finite coordinate) fails alone on its admission worker: its
   result carries its status, and the other jobs of the stream finish with the
   results they have alone.
+* A bounded device wait that runs out: under ERP_FLAG_EXPIRE_WAITS the row
+  pass's wait on its bulk copies gives up at once (no copy stalls: each is
+  still drained with the full limit), so the timeout path runs -- the status
+  bit, the context's retirement, ERP_ETIMEDOUT on the host -- and the device
+  stays usable.
 """
 import numpy as np
 import pytest
@@ -54,6 +59,35 @@ def test_nan_position_retires_with_enan(R):
     with R.Placement(d, (64, 64), 1.0, start_mode=1) as pl:
         it, last = pl.run(5)
         assert it == 5 and np.isfinite(last["hpwl"])
+
+
+@pytest.mark.parametrize("bins", [(64, 64), (256, 128), (512, 512)])
+def test_bounded_wait_runs_out(R, bins):
+    """Row passes of both copy-staged forms (one warp per row up to 256 bins, four
+    warps per row from 512): the step reports ERP_ETIMEDOUT, the context stays
+    retired, and a context without the flag on the same design runs normally."""
+    d = small_synth(3000, seed=42)
+    with R.Placement(d, bins, 1.0, start_mode=1, flags=R.lib.FLAG_EXPIRE_WAITS) as pl:
+        with pytest.raises(R.ErpError) as e:
+            pl.step()
+        assert e.value.status == R.lib.ETIMEDOUT
+        assert "wait limit" in str(e.value)
+        x0, y0 = pl.positions()
+        with pytest.raises(R.ErpError) as e2:   # retired: later steps report the same, move nothing
+            pl.step()
+        assert e2.value.status == R.lib.ETIMEDOUT
+        x1, y1 = pl.positions()
+        assert np.array_equal(x0, x1) and np.array_equal(y0, y1)
+    with R.Placement(d, bins, 1.0, start_mode=1) as pl:
+        it, last = pl.run(5)
+        assert it == 5 and np.isfinite(last["hpwl"])
+
+
+def test_unknown_flags_are_rejected(R):
+    d = small_synth(500, seed=43)
+    with pytest.raises(R.ErpError) as e:
+        R.Placement(d, (64, 64), 1.0, flags=2)
+    assert e.value.status == R.lib.EINVAL
 
 
 def test_server_isolates_failed_jobs(R):

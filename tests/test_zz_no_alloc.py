@@ -29,7 +29,10 @@ def R(built):
     return R
 
 
-@pytest.mark.parametrize("m,n,bw,bh", [(512, 512, 1.3, 1.1), (64, 256, 0.7, 2.1)])
+# group and warp transform forms (512, 64-256), and the generic radix-2 forms
+# (sides 16, 32 and 4096) with the largest twiddle-table offsets
+@pytest.mark.parametrize("m,n,bw,bh", [(512, 512, 1.3, 1.1), (64, 256, 0.7, 2.1), (4096, 64, 0.9, 1.4),
+                                       (32, 4096, 1.1, 0.8), (16, 16, 1.0, 1.0)])
 def test_noalloc_matches_allocating_solve(R, m, n, bw, bh):
     import torch
     lib = R.lib.load()
