@@ -150,6 +150,14 @@ static void initial_density(erpo_state *s) {
     for (size_t k = 0; k < mn; ++k) s->initial_map[k] = s->initial_map[k] * s->target_density;
 }
 
+/* The state's thread count for the parallel regions that follow (num_threads
+ * <= 0: every processor).  OpenMP's thread count is one setting of the calling
+ * thread, so each entry point sets it again: two oracles with different counts
+ * can be used in turn. */
+static void use_threads(const erpo_state *s) {
+    omp_set_num_threads(s->p.num_threads > 0 ? s->p.num_threads : omp_get_num_procs());
+}
+
 erpo_state *erpo_create(const erpo_design *d, const erpo_params *p) {
     if (!d || !p) return NULL;
     int m = p->num_bins_x, n = p->num_bins_y;
@@ -157,7 +165,7 @@ erpo_state *erpo_create(const erpo_design *d, const erpo_params *p) {
     erpo_state *s = (erpo_state *)calloc(1, sizeof(erpo_state));
     s->d = *d;
     s->p = *p;
-    if (p->num_threads > 0) omp_set_num_threads(p->num_threads);
+    use_threads(s);
     s->m = m; s->n = n;
     size_t N = (size_t)d->num_nodes, P = (size_t)d->num_pins, E = (size_t)d->num_nets;
     size_t mn = (size_t)m * n;
@@ -362,6 +370,7 @@ static float wa_net(erpo_state *s, int e, float inv_gamma, float def_min_x, floa
 }
 
 float erpo_compute_hpwl(erpo_state *s, float gamma) {
+    use_threads(s);
     const erpo_design *d = &s->d;
     long N = d->num_nodes, P = d->num_pins, E = d->num_nets, NM = d->num_movable;
     /* reset (src/hpwl.rs:77-84) */
@@ -542,6 +551,7 @@ static void electric_force(erpo_state *s) {
 }
 
 float erpo_compute_potential(erpo_state *s, int32_t iteration, float *energy_out) {
+    use_threads(s);
     int m = s->m, n = s->n;
     size_t mn = (size_t)m * n;
     movable_density(s, iteration);
@@ -590,6 +600,7 @@ float erpo_compute_potential(erpo_state *s, int32_t iteration, float *energy_out
 /* ---------------- optimiser: src/nesterov.rs ---------------- */
 
 void erpo_nesterov(erpo_state *s, int32_t iteration) {
+    use_threads(s);
     const erpo_design *d = &s->d;
     long NM = d->num_movable;
     float one = 1.0f, two = one + one, four = two + two;
@@ -718,6 +729,7 @@ int32_t erpo_should_stop(const erpo_state *s) {
 }
 
 int32_t erpo_step(erpo_state *s, erpo_step_stats *st) {
+    use_threads(s);
     float hp = erpo_compute_hpwl(s, s->gamma);
     float energy = 0;
     float ovf = erpo_compute_potential(s, s->iteration, &energy);

@@ -10,6 +10,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 
 #include <atomic>
@@ -238,6 +239,8 @@ struct WaClasses {
 __global__ void __launch_bounds__(kThreads, 4) k_wa(WaArgs a, WaClasses cl, float gamma_arg,
                                                  double *__restrict__ partials, DevState *st) {
     __shared__ double shr[kThreads / 32];
+    dep_wait();
+    dep_trigger();
     if (st->done) return;
     const float gamma = gamma_arg > 0.f ? gamma_arg : st->gamma;
     a.inv_gamma = 1.0f / gamma;                        // src/hpwl.rs:166
@@ -291,6 +294,8 @@ __global__ void __launch_bounds__(kThreads) k_wl_gather(int NM, const int32_t *_
                                                         const float2 *__restrict__ g,
                                                         float *__restrict__ gx, float *__restrict__ gy,
                                                         const DevState *__restrict__ st) {
+    dep_wait();
+    dep_trigger();
     if (st->done) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
         float sx = 0.0f, sy = 0.0f;
@@ -364,21 +369,24 @@ static_assert(kSortTile + 2 * kSortPad == kWin, "the window covers a tile and it
 constexpr int kTableLog = 9, kTable = 1 << kTableLog;   // out-of-window bin table (open, no probing)
 constexpr unsigned kEmpty = 0xffffffffu;                 // bin indices are < 4096 * 4096
 constexpr int kMaxCellsPerBlock = 2048;
+constexpr int kAggSide = 5;   // warp-aggregated scatter: the warp's cells within kAggSide x kAggSide bins
 constexpr unsigned long long kPiece = (1ull << 21) - 1;
-// The contribution c = rint((px * py) * 2^S) of one (cell, bin) pair to the
-// block's window, its bin table, or global memory, as PLANES 21-bit pieces.
+// Adds the integer s0 + s1 2^21 + s2 2^42 to bin (bx, by): into the block's
+// window plane by plane, else into its bin table, else into global memory.
+// (s0, s1, s2) are the 21-bit pieces of one contribution c = rint((px * py) *
+// 2^S), or their sums over a warp's lanes (each below 2^26).  Every plane's
+// total over a block stays below 2^32: a bin receives at most one contribution
+// per cell, and a block owns at most kMaxCellsPerBlock = 2^11 cells.
 template <int PLANES>
-__device__ __forceinline__ void scatter_add(int bx, int by, unsigned long long c, int wox, int woy, int n,
-                                            unsigned *win, unsigned *tkey, unsigned *tplane,
+__device__ __forceinline__ void scatter_add(int bx, int by, unsigned s0, unsigned s1, unsigned s2, int wox,
+                                            int woy, int n, unsigned *win, unsigned *tkey, unsigned *tplane,
                                             unsigned long long *__restrict__ map) {
     const unsigned wx = (unsigned)(bx - wox), wy = (unsigned)(by - woy);
     if (wx < (unsigned)kWin && wy < (unsigned)kWin) {
         unsigned *w = win + wx * kWin + wy;
-        atomicAdd(w, (unsigned)(c & kPiece));
-        if (c >> 21) {
-            atomicAdd(w + kWin * kWin, (unsigned)((c >> 21) & kPiece));
-            if (PLANES == 3 && (c >> 42)) atomicAdd(w + 2 * kWin * kWin, (unsigned)(c >> 42));
-        }
+        if (s0) atomicAdd(w, s0);
+        if (s1) atomicAdd(w + kWin * kWin, s1);
+        if (PLANES == 3 && s2) atomicAdd(w + 2 * kWin * kWin, s2);
         return;
     }
     // outside the window: the block's bin table, else global memory
@@ -391,37 +399,21 @@ __device__ __forceinline__ void scatter_add(int bx, int by, unsigned long long c
     }
     if (k == bin) {
         unsigned *t = tplane + slot;
-        atomicAdd(t, (unsigned)(c & kPiece));
-        if (c >> 21) {
-            atomicAdd(t + kTable, (unsigned)((c >> 21) & kPiece));
-            if (PLANES == 3 && (c >> 42)) atomicAdd(t + 2 * kTable, (unsigned)(c >> 42));
-        }
+        if (s0) atomicAdd(t, s0);
+        if (s1) atomicAdd(t + kTable, s1);
+        if (PLANES == 3 && s2) atomicAdd(t + 2 * kTable, s2);
     } else {
-        atomicAdd(map + bin, c);
+        atomicAdd(map + bin, (unsigned long long)s0 + ((unsigned long long)s1 << 21) +
+                                 (PLANES == 3 ? (unsigned long long)s2 << 42 : 0ull));
     }
 }
 
-// Overlaps of one cell with up to four consecutive bins starting at k0 (zero
-// beyond `count`), shifted so that the first nonzero one comes first; returns
-// the length of the run up to the last nonzero overlap and advances k0 past the
-// leading zeros.  Zeros inside the run only give zero contributions, which add
-// nothing to an integer sum.
-__device__ __forceinline__ int overlap_run4(float x, float s, int &k0, int count, float bs, float mul,
-                                            float (&t)[4]) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) t[j] = j < count ? mul * tri_clamped(x, s, k0 + j, bs) : 0.0f;
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        if (t[0] == 0.0f) {
-            t[0] = t[1]; t[1] = t[2]; t[2] = t[3]; t[3] = 0.0f;
-            ++k0;
-        }
-    }
-    return t[3] != 0.0f ? 4 : t[2] != 0.0f ? 3 : t[1] != 0.0f ? 2 : t[0] != 0.0f ? 1 : 0;
-}
-
-__device__ __forceinline__ float pick4(const float (&t)[4], int j) {
-    return j == 0 ? t[0] : j == 1 ? t[1] : j == 2 ? t[2] : t[3];
+template <int PLANES>
+__device__ __forceinline__ void scatter_add(int bx, int by, unsigned long long c, int wox, int woy, int n,
+                                            unsigned *win, unsigned *tkey, unsigned *tplane,
+                                            unsigned long long *__restrict__ map) {
+    scatter_add<PLANES>(bx, by, (unsigned)(c & kPiece), (unsigned)((c >> 21) & kPiece),
+                        PLANES == 3 ? (unsigned)(c >> 42) : 0u, wox, woy, n, win, tkey, tplane, map);
 }
 
 template <int PLANES>
@@ -434,6 +426,14 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
     unsigned *win = dsm;                                  // window planes: bits 0-20, 21-41 (, 42-62)
     unsigned *tkey = dsm + PLANES * kWin * kWin;          // bin table: keys (bin index or kEmpty)
     unsigned *tplane = tkey + kTable;                     // bin table: planes
+    {   // shared memory only: overlaps the previous kernel's tail
+        uint4 *w4 = reinterpret_cast<uint4 *>(dsm);
+        for (int k = threadIdx.x; k < PLANES * kWin * kWin / 4; k += blockDim.x) w4[k] = make_uint4(0u, 0u, 0u, 0u);
+        for (int k = threadIdx.x; k < kTable; k += blockDim.x) tkey[k] = kEmpty;
+        for (int k = threadIdx.x; k < PLANES * kTable; k += blockDim.x) tplane[k] = 0u;
+    }
+    dep_wait();
+    dep_trigger();
     if (st->done) return;
     const int per = ((NM + gridDim.x - 1) / gridDim.x + 31) & ~31;   // <= kMaxCellsPerBlock (launcher)
     const int c0 = blockIdx.x * per, c1 = min(c0 + per, NM);
@@ -445,12 +445,6 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
     }
     wox = max(0, min(wox, m - kWin));
     woy = max(0, min(woy, n - kWin));
-    {
-        uint4 *w4 = reinterpret_cast<uint4 *>(dsm);
-        for (int k = threadIdx.x; k < PLANES * kWin * kWin / 4; k += blockDim.x) w4[k] = make_uint4(0u, 0u, 0u, 0u);
-        for (int k = threadIdx.x; k < kTable; k += blockDim.x) tkey[k] = kEmpty;
-        for (int k = threadIdx.x; k < PLANES * kTable; k += blockDim.x) tplane[k] = 0u;
-    }
     __syncthreads();
     for (int base = c0; base < c1; base += blockDim.x) {
         const int p = base + threadIdx.x;
@@ -474,26 +468,44 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
             nx = max(xh - xl, 0);
             ny = max(yh - yl, 0);
         }
-        if (nx <= 4 && ny <= 4) {
-            // standard cells: every overlap computed once, the cell's (x, y) pairs
-            // walked in one flat loop (px = r * x-overlap, py = y-overlap; the
-            // contribution rint((px * py) * 2^S) as in the oracle)
-            float tx[4], ty[4];
-            const int cx = overlap_run4(xi, sxi, bxl, nx, bw, r, tx);
-            const int cy = overlap_run4(yi, syi, byl, ny, bh, 1.0f, ty);
-            const int cnt = cx * cy;
-            int dx = 0, dy = 0;
-            for (int k = 0; k < cnt; ++k) {
-                const float px = pick4(tx, dx), py = pick4(ty, dy);
-                const unsigned long long c = (unsigned long long)fxp_rint_u64((px * py) * scale);
-                if (c) scatter_add<PLANES>(bxl + dx, byl + dy, c, wox, woy, n, win, tkey, tplane, map);
-                if (++dy == cy) {
-                    dy = 0;
-                    ++dx;
+        // the bins the warp's cells reach together (their full ranges)
+        const unsigned full = 0xffffffffu;
+        const bool any = nx > 0 && ny > 0;
+        const int ax = __reduce_min_sync(full, any ? bxl : INT_MAX);
+        const int ay = __reduce_min_sync(full, any ? byl : INT_MAX);
+        const int ex = __reduce_max_sync(full, any ? bxl + nx : INT_MIN);
+        const int ey = __reduce_max_sync(full, any ? byl + ny : INT_MIN);
+        if (ax != INT_MAX && ex - ax <= kAggSide && ey - ay <= kAggSide) {
+            // Warp-aggregated atomics.  The warp's cells crowd into at most
+            // kAggSide x kAggSide bins (early in the run most cells sit within a
+            // few bins of the die centre).  Bin by bin, every lane forms its
+            // contribution -- zero outside its own range -- the warp sums the
+            // 21-bit pieces, and one lane adds the sums: one atomic per bin and
+            // plane instead of up to 32 contending ones.  Integer sums, so the
+            // bits are those of the lanes' own adds.
+            const int lane = threadIdx.x & 31;
+            float pyk[kAggSide];
+#pragma unroll
+            for (int k = 0; k < kAggSide; ++k) {
+                const int by = ay + k;
+                pyk[k] = (by >= byl && by < byl + ny) ? tri_clamped(yi, syi, by, bh) : 0.0f;
+            }
+            for (int bx = ax; bx < ex; ++bx) {
+                const float px = (bx >= bxl && bx < bxl + nx) ? r * tri_clamped(xi, sxi, bx, bw) : 0.0f;
+#pragma unroll
+                for (int k = 0; k < kAggSide; ++k) {
+                    if (ay + k < ey) {   // warp-uniform
+                        const unsigned long long c = (unsigned long long)fxp_rint_u64((px * pyk[k]) * scale);
+                        const unsigned s0 = __reduce_add_sync(full, (unsigned)(c & kPiece));
+                        const unsigned s1 = __reduce_add_sync(full, (unsigned)((c >> 21) & kPiece));
+                        const unsigned s2 = PLANES == 3 ? __reduce_add_sync(full, (unsigned)(c >> 42)) : 0u;
+                        if (lane == 0 && (s0 | s1 | s2))
+                            scatter_add<PLANES>(bx, ay + k, s0, s1, s2, wox, woy, n, win, tkey, tplane, map);
+                    }
                 }
             }
         } else {
-            // larger cells: the bin columns and rows in full
+            // spread cells: each lane its own bin columns and rows
             for (int dx = 0; dx < nx; ++dx) {
                 const int bx = bxl + dx;
                 const float px = r * tri_clamped(xi, sxi, bx, bw);
@@ -683,6 +695,8 @@ __global__ void __launch_bounds__(kThreads) k_force(
     int rescale, const float *__restrict__ wlgx, const float *__restrict__ wlgy,
     double *__restrict__ partials, DevState *st) {
     __shared__ double shr[kThreads / 32];
+    dep_wait();
+    dep_trigger();
     if (st->done) return;
     // the field gathered over cell i's bins (src/eforce.rs)
     auto force = [&](int i, float nx, float ny, float sx, float sy, float r) {
@@ -842,6 +856,8 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_grad(
     const float *__restrict__ y, const float *__restrict__ px, const float *__restrict__ py,
     float *__restrict__ pgx, float *__restrict__ pgy, double *__restrict__ partials, DevState *st) {
     __shared__ double shr[kThreads / 32];
+    dep_wait();
+    dep_trigger();
     if (st->done) return;
     const float dw = st->dw;
     float numf = 0.0f, denf = 0.0f;
@@ -910,6 +926,8 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_update(
     float *__restrict__ x, float *__restrict__ y, float *__restrict__ px, float *__restrict__ py,
     const float *__restrict__ gx, const float *__restrict__ gy, float2 *__restrict__ xy,
     const DevState *__restrict__ st) {
+    dep_wait();
+    dep_trigger();
     if (st->done) return;
     const float alpha = st->alpha, beta = st->beta;
     const int n4 = NM >> 2;
@@ -976,6 +994,8 @@ struct SchedLogs {
 // Scheduler::update + should_stop (src/scheduler.rs:68-130) in FP64, plus the
 // step record, the non-finite check and the retire-at-overflow flag.
 __global__ void k_scheduler(int use_args, float hpwl_arg, float ovf_arg, SchedLogs lg, DevState *st) {
+    dep_wait();
+    dep_trigger();
     if (blockIdx.x != 0) return;
     if (st->done) return;   // warp-uniform
     const float hpwl = use_args ? hpwl_arg : st->hpwl_f;
@@ -1100,12 +1120,12 @@ void launch_wirelength(Ctx &c, float gamma_arg) {
         k_wl_zero<<<1, 32, 0, c.stream>>>(c.st);
         return;
     }
-    k_wa<<<blocks, kThreads, 0, c.stream>>>(a, cl, gamma_arg, c.partials, c.st);
+    launch_dep(k_wa, blocks, kThreads, 0, c.stream, a, cl, gamma_arg, c.partials, c.st);
 }
 
 void launch_wl_gather(Ctx &c) {
-    k_wl_gather<<<grid_for(c.NM), kThreads, 0, c.stream>>>(c.NM, c.cell_slot_ptr, c.cell_slots,
-                                                           c.slot_grad, c.wlgx, c.wlgy, c.st);
+    launch_dep(k_wl_gather, grid_for(c.NM), kThreads, 0, c.stream, c.NM, c.cell_slot_ptr, c.cell_slots,
+               c.slot_grad, c.wlgx, c.wlgy, c.st);
 }
 
 // Blocks of the scatter.  Alone, a context spreads its cells over up to 608
@@ -1119,9 +1139,9 @@ void launch_density_scatter(Ctx &c) {
                                       : std::max(grid_for(c.NM, 152 * 4), floor_g);
     const int nty = (c.n + kSortTile - 1) / kSortTile;
     auto kern = c.scatter_planes == 2 ? k_density_scatter<2> : k_density_scatter<3>;
-    kern<<<g, kThreads, density_scatter_smem(c.scatter_planes), c.stream>>>(
-        c.NM, c.perm, c.xy, c.soff, c.sratio, c.skey, nty, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw,
-        c.inv_bh, c.fixed_scale, c.dmap, c.st);
+    launch_dep(kern, g, kThreads, density_scatter_smem(c.scatter_planes), c.stream, c.NM, c.perm, c.xy, c.soff,
+               c.sratio, c.skey, nty, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw, c.inv_bh, c.fixed_scale, c.dmap,
+               c.st);
 }
 
 void launch_scatter_order(Ctx &c, cudaStream_t s) {
@@ -1180,9 +1200,9 @@ static int fit(int need, const std::atomic<int> &resident_a) {
 }
 
 void launch_force(Ctx &c, int rescale) {
-    k_force<<<fit(grid_for(c.NM, 152 * 16), g_res_force), kThreads, 0, c.stream>>>(
-        c.NM, c.perm, c.xy, c.soff, c.sratio, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w, c.bin_h,
-        c.inv_bw, c.inv_bh, c.fx, c.fy, c.dgx, c.dgy, rescale, c.wlgx, c.wlgy, c.partials, c.st);
+    launch_dep(k_force, fit(grid_for(c.NM, 152 * 16), g_res_force), kThreads, 0, c.stream,
+               c.NM, c.perm, c.xy, c.soff, c.sratio, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w,
+               c.bin_h, c.inv_bw, c.inv_bh, c.fx, c.fy, c.dgx, c.dgy, rescale, c.wlgx, c.wlgy, c.partials, c.st);
 }
 
 void launch_energy(Ctx &c) {
@@ -1198,11 +1218,10 @@ void launch_nesterov(Ctx &c, int iter_arg) {
                                                    c.partials, c.st);
     }
     const int g4 = grid_for((c.NM + 3) / 4);
-    k_nesterov_grad<<<fit(g4, g_res_grad), kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx, c.dgy, c.w,
-                                                  c.h, c.npins, c.x, c.y, c.prev_x, c.prev_y,
-                                                  c.prev_gx, c.prev_gy, c.partials, c.st);
-    k_nesterov_update<<<fit(g4, g_res_update), kThreads, 0, c.stream>>>(c.NM, c.w, c.h, c.die_w, c.die_h, c.x, c.y,
-                                                    c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.xy, c.st);
+    launch_dep(k_nesterov_grad, fit(g4, g_res_grad), kThreads, 0, c.stream, c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx,
+               c.dgy, c.w, c.h, c.npins, c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.partials, c.st);
+    launch_dep(k_nesterov_update, fit(g4, g_res_update), kThreads, 0, c.stream, c.NM, c.w, c.h, c.die_w, c.die_h,
+               c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.xy, c.st);
 }
 
 cudaError_t place_occupancy() {
@@ -1282,7 +1301,7 @@ void launch_scheduler(Ctx &c, int use_args, float hpwl, float overflow) {
     // update_density_weight's bases 0.9999 and 1.05, update_gamma's 10
     // (src/scheduler.rs:92-130)
     static const SchedLogs lg = {std::log(0.9999), std::log(1.05), std::log(10.0)};
-    k_scheduler<<<1, 32, 0, c.stream>>>(use_args, hpwl, overflow, lg, c.st);
+    launch_dep(k_scheduler, 1, 32, 0, c.stream, use_args, hpwl, overflow, lg, c.st);
 }
 
 }  // namespace erp

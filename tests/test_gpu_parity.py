@@ -256,6 +256,63 @@ def test_reference_start_first_step(R, O):
     assert abs(g.last_stats["overflow"] - so["overflow"]) <= 1e-6
 
 
+def _piled(d, sigma_bins, bins, seed):
+    """Movable cells around the die centre, Gaussian with sigma in bins."""
+    rng = np.random.default_rng(seed)
+    x, y = d.x.copy(), d.y.copy()
+    NM = d.num_movable
+    bw, bh = d.die_w / bins[0], d.die_h / bins[1]
+    x[:NM] = (d.die_w / 2 - d.w[:NM] / 2 + rng.normal(0, sigma_bins * bw, NM)).astype(np.float32)
+    y[:NM] = (d.die_h / 2 - d.h[:NM] / 2 + rng.normal(0, sigma_bins * bh, NM)).astype(np.float32)
+    return x, y
+
+
+def _with_wide_cells(d, cells, factor):
+    """The same design with some movable cells widened (pin offsets stay inside)."""
+    import copy
+    e = copy.deepcopy(d)
+    e.w = e.w.copy()
+    e.w[cells] *= factor
+    NM = e.num_movable
+    mov = float(np.sum(e.w[:NM].astype(np.float64) * e.h[:NM]))
+    fixed = float(np.sum(e.w[NM:].astype(np.float64) * e.h[NM:]))
+    e.movable_area = mov
+    e.cell_utilization = mov / (e.die_w * e.die_h - fixed)
+    return e
+
+
+@pytest.mark.parametrize("case", ["centre", "piled_0.3", "piled_2", "spread", "wide_cells_piled", "wide_cells_spread"])
+def test_density_map_crowded_and_wide_cells_bit_exact(R, O, case):
+    """The scatter's three paths against the oracle's fixed-point replay, bit for
+    bit: warps whose cells crowd into at most 4 x 4 bins (one warp-summed atomic
+    per bin), warps of spread standard cells (one lane per cell), and warps that
+    hold a cell spanning more than 4 bins (full bin loops)."""
+    d = small_synth(20000, seed=61, macros=2, io=200)
+    bins = (128, 128)
+    if case.startswith("wide"):
+        d = _with_wide_cells(d, np.arange(0, 20000, 97), 12.0)
+    if case == "centre":
+        xy = (d.x.copy(), d.y.copy())
+        NM = d.num_movable
+        xy[0][:NM] = (d.die_w / 2 - d.w[:NM] / 2).astype(np.float32)
+        xy[1][:NM] = (d.die_h / 2 - d.h[:NM] / 2).astype(np.float32)
+    elif case in ("piled_0.3", "wide_cells_piled"):
+        xy = _piled(d, 0.3, bins, 5)
+    elif case == "piled_2":
+        xy = _piled(d, 2.0, bins, 6)
+    else:
+        xy = spread_positions(d, seed=7)
+    o, g = make_pair(R, O, d, *bins, xy=xy)
+    try:
+        _, ovo = o.compute_potential(0)
+        _, ovg = g.compute_potential(0)
+        assert np.array_equal(g.array("DENSITY_I64"), o.get("density_i64"))
+        assert abs(ovg - ovo) <= 1e-6 * max(abs(ovo), 1e-12)
+    finally:
+        g.close()
+        o.close()
+
+
 def test_run_retires_at_overflow(R):
     d = small_synth(3000, seed=23)
     g = R.Placement(d, (64, 64), 1.0)
