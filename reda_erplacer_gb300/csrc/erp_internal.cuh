@@ -14,32 +14,6 @@ namespace erp {
 
 constexpr int kThreads = 256;
 
-// Programmatic dependent launch.  The kernels of a step are launched with
-// launch_dep(): the next kernel on the stream may then be scheduled while its
-// predecessor drains.  Each such kernel calls dep_wait() before it reads or
-// writes global memory that another kernel of the step touches -- the wait
-// returns once the preceding grid has completed and its writes are visible --
-// and dep_trigger() to let its own successor be scheduled once all of its
-// blocks have started.  Launched any other way both are no-ops.
-__device__ __forceinline__ void dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void dep_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-
-template <typename... P, typename... A>
-inline cudaError_t launch_dep(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
-                              A &&...args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kernel, static_cast<A &&>(args)...);
-}
-
 // Device-resident scalars.  Every quantity the reference keeps in Scheduler /
 // Nesterov (src/scheduler.rs:37-50, src/nesterov.rs:6-13) plus the reductions
 // of the current step, so that a whole Placement::step runs without a host

@@ -239,8 +239,6 @@ struct WaClasses {
 __global__ void __launch_bounds__(kThreads, 4) k_wa(WaArgs a, WaClasses cl, float gamma_arg,
                                                  double *__restrict__ partials, DevState *st) {
     __shared__ double shr[kThreads / 32];
-    dep_wait();
-    dep_trigger();
     if (st->done) return;
     const float gamma = gamma_arg > 0.f ? gamma_arg : st->gamma;
     a.inv_gamma = 1.0f / gamma;                        // src/hpwl.rs:166
@@ -294,8 +292,6 @@ __global__ void __launch_bounds__(kThreads) k_wl_gather(int NM, const int32_t *_
                                                         const float2 *__restrict__ g,
                                                         float *__restrict__ gx, float *__restrict__ gy,
                                                         const DevState *__restrict__ st) {
-    dep_wait();
-    dep_trigger();
     if (st->done) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
         float sx = 0.0f, sy = 0.0f;
@@ -432,8 +428,6 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
         for (int k = threadIdx.x; k < kTable; k += blockDim.x) tkey[k] = kEmpty;
         for (int k = threadIdx.x; k < PLANES * kTable; k += blockDim.x) tplane[k] = 0u;
     }
-    dep_wait();
-    dep_trigger();
     if (st->done) return;
     const int per = ((NM + gridDim.x - 1) / gridDim.x + 31) & ~31;   // <= kMaxCellsPerBlock (launcher)
     const int c0 = blockIdx.x * per, c1 = min(c0 + per, NM);
@@ -695,8 +689,6 @@ __global__ void __launch_bounds__(kThreads) k_force(
     int rescale, const float *__restrict__ wlgx, const float *__restrict__ wlgy,
     double *__restrict__ partials, DevState *st) {
     __shared__ double shr[kThreads / 32];
-    dep_wait();
-    dep_trigger();
     if (st->done) return;
     // the field gathered over cell i's bins (src/eforce.rs)
     auto force = [&](int i, float nx, float ny, float sx, float sy, float r) {
@@ -856,8 +848,6 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_grad(
     const float *__restrict__ y, const float *__restrict__ px, const float *__restrict__ py,
     float *__restrict__ pgx, float *__restrict__ pgy, double *__restrict__ partials, DevState *st) {
     __shared__ double shr[kThreads / 32];
-    dep_wait();
-    dep_trigger();
     if (st->done) return;
     const float dw = st->dw;
     float numf = 0.0f, denf = 0.0f;
@@ -926,8 +916,6 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_update(
     float *__restrict__ x, float *__restrict__ y, float *__restrict__ px, float *__restrict__ py,
     const float *__restrict__ gx, const float *__restrict__ gy, float2 *__restrict__ xy,
     const DevState *__restrict__ st) {
-    dep_wait();
-    dep_trigger();
     if (st->done) return;
     const float alpha = st->alpha, beta = st->beta;
     const int n4 = NM >> 2;
@@ -994,8 +982,6 @@ struct SchedLogs {
 // Scheduler::update + should_stop (src/scheduler.rs:68-130) in FP64, plus the
 // step record, the non-finite check and the retire-at-overflow flag.
 __global__ void k_scheduler(int use_args, float hpwl_arg, float ovf_arg, SchedLogs lg, DevState *st) {
-    dep_wait();
-    dep_trigger();
     if (blockIdx.x != 0) return;
     if (st->done) return;   // warp-uniform
     const float hpwl = use_args ? hpwl_arg : st->hpwl_f;
@@ -1120,11 +1106,11 @@ void launch_wirelength(Ctx &c, float gamma_arg) {
         k_wl_zero<<<1, 32, 0, c.stream>>>(c.st);
         return;
     }
-    launch_dep(k_wa, blocks, kThreads, 0, c.stream, a, cl, gamma_arg, c.partials, c.st);
+    k_wa<<<blocks, kThreads, 0, c.stream>>>(a, cl, gamma_arg, c.partials, c.st);
 }
 
 void launch_wl_gather(Ctx &c) {
-    launch_dep(k_wl_gather, grid_for(c.NM), kThreads, 0, c.stream, c.NM, c.cell_slot_ptr, c.cell_slots,
+    k_wl_gather<<<grid_for(c.NM), kThreads, 0, c.stream>>>(c.NM, c.cell_slot_ptr, c.cell_slots,
                c.slot_grad, c.wlgx, c.wlgy, c.st);
 }
 
@@ -1139,7 +1125,7 @@ void launch_density_scatter(Ctx &c) {
                                       : std::max(grid_for(c.NM, 152 * 4), floor_g);
     const int nty = (c.n + kSortTile - 1) / kSortTile;
     auto kern = c.scatter_planes == 2 ? k_density_scatter<2> : k_density_scatter<3>;
-    launch_dep(kern, g, kThreads, density_scatter_smem(c.scatter_planes), c.stream, c.NM, c.perm, c.xy, c.soff,
+    kern<<<g, kThreads, density_scatter_smem(c.scatter_planes), c.stream>>>(c.NM, c.perm, c.xy, c.soff,
                c.sratio, c.skey, nty, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw, c.inv_bh, c.fixed_scale, c.dmap,
                c.st);
 }
@@ -1200,7 +1186,7 @@ static int fit(int need, const std::atomic<int> &resident_a) {
 }
 
 void launch_force(Ctx &c, int rescale) {
-    launch_dep(k_force, fit(grid_for(c.NM, 152 * 16), g_res_force), kThreads, 0, c.stream,
+    k_force<<<fit(grid_for(c.NM, 152 * 16), g_res_force), kThreads, 0, c.stream>>>(
                c.NM, c.perm, c.xy, c.soff, c.sratio, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w,
                c.bin_h, c.inv_bw, c.inv_bh, c.fx, c.fy, c.dgx, c.dgy, rescale, c.wlgx, c.wlgy, c.partials, c.st);
 }
@@ -1218,9 +1204,9 @@ void launch_nesterov(Ctx &c, int iter_arg) {
                                                    c.partials, c.st);
     }
     const int g4 = grid_for((c.NM + 3) / 4);
-    launch_dep(k_nesterov_grad, fit(g4, g_res_grad), kThreads, 0, c.stream, c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx,
+    k_nesterov_grad<<<fit(g4, g_res_grad), kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx,
                c.dgy, c.w, c.h, c.npins, c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.partials, c.st);
-    launch_dep(k_nesterov_update, fit(g4, g_res_update), kThreads, 0, c.stream, c.NM, c.w, c.h, c.die_w, c.die_h,
+    k_nesterov_update<<<fit(g4, g_res_update), kThreads, 0, c.stream>>>(c.NM, c.w, c.h, c.die_w, c.die_h,
                c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.xy, c.st);
 }
 
@@ -1301,7 +1287,7 @@ void launch_scheduler(Ctx &c, int use_args, float hpwl, float overflow) {
     // update_density_weight's bases 0.9999 and 1.05, update_gamma's 10
     // (src/scheduler.rs:92-130)
     static const SchedLogs lg = {std::log(0.9999), std::log(1.05), std::log(10.0)};
-    launch_dep(k_scheduler, 1, 32, 0, c.stream, use_args, hpwl, overflow, lg, c.st);
+    k_scheduler<<<1, 32, 0, c.stream>>>(use_args, hpwl, overflow, lg, c.st);
 }
 
 }  // namespace erp

@@ -73,8 +73,6 @@ __global__ void __launch_bounds__(kThreads) k_rows_dct(
     const float *__restrict__ initial, float fixed_inv, float coef, float inv_area, int zero_map,
     float *__restrict__ rho_out, float *__restrict__ t1, double *__restrict__ partials,
     DevState *__restrict__ st, double movable_area) {
-    dep_wait();
-    dep_trigger();
     if (st && st->done) return;
     extern __shared__ __align__(16) float2 sm[];
     float2 *tw = sm;
@@ -146,8 +144,6 @@ __global__ void __launch_bounds__(kThreads) k_cols(
     const float *__restrict__ wu, const float *__restrict__ wv, const float *__restrict__ t1,
     float *__restrict__ tx, float *__restrict__ ty, float *__restrict__ tp, float scale4,
     const DevState *__restrict__ st) {
-    dep_wait();
-    dep_trigger();
     if (st && st->done) return;
     constexpr int CB = 2 * CP;
     extern __shared__ __align__(16) float2 sm[];
@@ -242,8 +238,6 @@ __global__ void __launch_bounds__(kThreads) k_rows_inv(
     const float *__restrict__ tx, const float *__restrict__ ty, const float *__restrict__ tp,
     float *__restrict__ fx, float *__restrict__ fy, float *__restrict__ psi,
     const DevState *__restrict__ st) {
-    dep_wait();
-    dep_trigger();
     if (st && st->done) return;
     extern __shared__ __align__(16) float2 sm[];
     float2 *tw = sm;
@@ -492,8 +486,6 @@ __global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
     float *__restrict__ rho_out, float *__restrict__ t1, double *__restrict__ partials,
     DevState *__restrict__ st, double movable_area) {
     constexpr int H = 32 * E, N = 2 * H;
-    dep_wait();
-    dep_trigger();
     if (st && st->done) return;
     extern __shared__ __align__(16) float2 sm[];
     __shared__ __align__(8) uint64_t bar[NW];
@@ -582,8 +574,6 @@ __global__ void __launch_bounds__(NW * 32) k_cols_w(
     const DevState *__restrict__ st) {
     constexpr int H = 32 * E, M = 2 * H;
     constexpr int S = NW + 1;   // tile row stride (odd: conflict-free row-wise access)
-    dep_wait();
-    dep_trigger();
     if (st && st->done) return;
     extern __shared__ __align__(16) float2 sm[];
     const AxisTables tb = load_tables<NW, H>(sm, tw_m, ek_m);
@@ -669,8 +659,6 @@ __global__ void __launch_bounds__(NW * 32) k_rows_inv_w(
     float *__restrict__ fx, float *__restrict__ fy, float *__restrict__ psi,
     const DevState *__restrict__ st) {
     constexpr int H = 32 * E, N = 2 * H;
-    dep_wait();
-    dep_trigger();
     if (st && st->done) return;
     extern __shared__ __align__(16) float2 sm[];
     const AxisTables tb = load_tables<NW, H>(sm, tw_n, ek_n);
@@ -829,8 +817,6 @@ __global__ void __launch_bounds__(G * kQ * 32) k_rows_dct_g(
     float *__restrict__ rho_out, float *__restrict__ t1, double *__restrict__ partials,
     DevState *__restrict__ st, double movable_area) {
     constexpr int H = 32 * E * kQ, N = 2 * H, PT = N / (32 * kQ);   // values per thread
-    dep_wait();
-    dep_trigger();
     if (st && st->done) return;
     extern __shared__ __align__(16) float2 sm[];
     __shared__ __align__(8) uint64_t bar[G];
@@ -923,8 +909,6 @@ __global__ void __launch_bounds__(G * kQ * 32) k_cols_g(
     float *__restrict__ tx, float *__restrict__ ty, float *__restrict__ tp, float scale4,
     const DevState *__restrict__ st) {
     constexpr int H = 32 * E * kQ, M = 2 * H, S = G + 1;   // tile row stride (odd)
-    dep_wait();
-    dep_trigger();
     if (st && st->done) return;
     extern __shared__ __align__(16) float2 sm[];
     const AxisTables tb = load_tables<G * kQ, H>(sm, tw_m, ek_m);
@@ -992,8 +976,6 @@ __global__ void __launch_bounds__(G * kQ * 32) k_rows_inv_g(
     float *__restrict__ fx, float *__restrict__ fy, float *__restrict__ psi,
     const DevState *__restrict__ st) {
     constexpr int H = 32 * E * kQ, N = 2 * H;
-    dep_wait();
-    dep_trigger();
     if (st && st->done) return;
     extern __shared__ __align__(16) float2 sm[];
     const AxisTables tb = load_tables<G * kQ, H>(sm, tw_n, ek_n);
@@ -1023,8 +1005,6 @@ __global__ void __launch_bounds__(kThreads) k_map_rho(size_t mn, unsigned long l
                                                       double *__restrict__ partials, DevState *__restrict__ st,
                                                       double movable_area) {
     __shared__ double shr[kThreads / 32];
-    dep_wait();
-    dep_trigger();
     if (st->done) return;
     Df ovf = df_zero();
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < mn; idx += (size_t)gridDim.x * blockDim.x) {
@@ -1158,19 +1138,19 @@ static cudaError_t prepare_g() {
 }
 template <int E>
 static void rows_dct_g(const SpectralPlan &p, const SpectralArgs &a, bool from_map) {
-    launch_dep(k_rows_dct_g<E, kRowGroups>, p.m / kRowGroups, kRowGroups * kQ * 32, rows_dct_g_smem<E>(), p.stream,
+    k_rows_dct_g<E, kRowGroups><<<p.m / kRowGroups, kRowGroups * kQ * 32, rows_dct_g_smem<E>(), p.stream>>>(
         p.m, p.tw_n, p.ek_n, a.rho_in, a.dmap, a.initial, a.fixed_inv, a.coef, a.inv_bin_area,
         a.zero_map ? 1 : 0, a.rho_out, p.t1, from_map ? a.partials : nullptr, a.st, a.movable_area);
 }
 template <int E>
 static void cols_g(const SpectralPlan &p, const SpectralArgs &a, float scale4, float *tp) {
-    launch_dep(k_cols_g<E, kColGroups>, p.n / kColGroups, kColGroups * kQ * 32, cols_g_smem<E>(), p.stream,
+    k_cols_g<E, kColGroups><<<p.n / kColGroups, kColGroups * kQ * 32, cols_g_smem<E>(), p.stream>>>(
         p.n, p.tw_m, p.ek_m, p.wu, p.wv, p.t1, p.tx, p.ty, tp, scale4, a.st);
 }
 template <int E>
 static void rows_inv_g(const SpectralPlan &p, const SpectralArgs &a, float *tp) {
     const int nk = tp ? 3 : 2;
-    launch_dep(k_rows_inv_g<E, kInvGroups>, p.m * nk / kInvGroups, kInvGroups * kQ * 32, rows_inv_g_smem<E>(), p.stream,
+    k_rows_inv_g<E, kInvGroups><<<p.m * nk / kInvGroups, kInvGroups * kQ * 32, rows_inv_g_smem<E>(), p.stream>>>(
         p.m, nk, p.tw_n, p.ek_n, p.tx, p.ty, tp, a.fx, a.fy, a.psi, a.st);
 }
 #define ERP_DISPATCH_G(side, FN, ...)           \
@@ -1208,19 +1188,19 @@ static bool warp_side(int v) { return v >= 64 && v <= 2048; }
 
 template <int E>
 static void rows_dct_w(const SpectralPlan &p, const SpectralArgs &a, bool from_map) {
-    launch_dep(k_rows_dct_w<E, kRowWarps>, p.m / kRowWarps, kRowWarps * 32, rows_dct_w_smem<E>(), p.stream,
+    k_rows_dct_w<E, kRowWarps><<<p.m / kRowWarps, kRowWarps * 32, rows_dct_w_smem<E>(), p.stream>>>(
         p.m, p.tw_n, p.ek_n, a.rho_in, a.dmap, a.initial, a.fixed_inv, a.coef, a.inv_bin_area,
         a.zero_map ? 1 : 0, a.rho_out, p.t1, from_map ? a.partials : nullptr, a.st, a.movable_area);
 }
 template <int E>
 static void cols_w(const SpectralPlan &p, const SpectralArgs &a, float scale4, float *tp) {
-    launch_dep(k_cols_w<E, kColWarps>, p.n / kColWarps, kColWarps * 32, cols_w_smem<E>(), p.stream,
+    k_cols_w<E, kColWarps><<<p.n / kColWarps, kColWarps * 32, cols_w_smem<E>(), p.stream>>>(
         p.n, p.tw_m, p.ek_m, p.wu, p.wv, p.t1, p.tx, p.ty, tp, scale4, a.st);
 }
 template <int E>
 static void rows_inv_w(const SpectralPlan &p, const SpectralArgs &a, float *tp) {
     const int nk = tp ? 3 : 2;
-    launch_dep(k_rows_inv_w<E, kRowWarps>, p.m * nk / kRowWarps, kRowWarps * 32, rows_w_smem<E>(), p.stream,
+    k_rows_inv_w<E, kRowWarps><<<p.m * nk / kRowWarps, kRowWarps * 32, rows_w_smem<E>(), p.stream>>>(
         p.m, nk, p.tw_n, p.ek_n, p.tx, p.ty, tp, a.fx, a.fy, a.psi, a.st);
 }
 
