@@ -31,7 +31,7 @@ CU_SOURCES = {
 }
 CPP_SOURCES = ["synth.cpp", "lefdef.cpp"]
 CLI_SOURCE = "erplacer_cli.cpp"   # the command-line driver, linked against the library
-HEADERS = ["erp_internal.cuh", "reduce.cuh", "bulk_copy.cuh"]
+HEADERS = ["erp_internal.cuh", "reduce.cuh", "bulk_copy.cuh", "dfloat.h", "fixedpoint.h", "binrange.h"]
 
 
 def _deps():
