@@ -162,7 +162,7 @@ erp_status validate(const erp_design *d, std::string &err) {
 
 void free_ctx(Ctx &c) {
     void *ptrs[] = {c.x, c.y, c.xy, c.w, c.h, c.npins, c.cw, c.ch, c.offx, c.offy, c.ratio, c.wlgx, c.wlgy,
-                    c.dgx, c.dgy, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.slot_cell, c.slot_off,
+                    c.dgp, c.pos, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.slot_cell, c.slot_off,
                     c.slot_grad, c.net_ptr, c.net_hpwl, c.cell_slot_ptr, c.cell_slots, c.dmap,
                     c.initial, c.rho, c.t1, c.tx, c.ty, c.tp, c.fx, c.fy, c.psi, c.tw_m, c.tw_n,
                     c.ek_m, c.ek_n, c.wu, c.wv, c.partials, c.st, c.perm, c.skey, c.soff, c.sratio,
@@ -398,7 +398,7 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     // --- device allocations ---
     const size_t mn = (size_t)c.m * c.n;
     float **cellarr[] = {&c.x, &c.y, &c.w, &c.h, &c.npins, &c.cw, &c.ch, &c.offx, &c.offy, &c.ratio,
-                         &c.wlgx, &c.wlgy, &c.dgx, &c.dgy, &c.prev_x, &c.prev_y, &c.prev_gx, &c.prev_gy};
+                         &c.wlgx, &c.wlgy, &c.prev_x, &c.prev_y, &c.prev_gx, &c.prev_gy};
     cudaStream_t s0 = c.stream;
     for (float **a : cellarr) CK(dalloc(a, (size_t)N + 4, s0));
     CK(dalloc(&c.xy, (size_t)N + 4, s0));
@@ -410,6 +410,8 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     CK(dalloc(&c.cell_slot_ptr, (size_t)NM + 1, s0));
     CK(dalloc(&c.cell_slots, hcell_slots.size(), s0));
     CK(dalloc(&c.perm, NM, s0));
+    CK(dalloc(&c.pos, (size_t)NM + 4, s0));
+    CK(dalloc(&c.dgp, (size_t)NM + 4, s0));
     CK(dalloc(&c.skey, NM, s0));
     CK(dalloc(&c.soff, NM, s0));
     CK(dalloc(&c.sratio, NM, s0));
@@ -445,8 +447,10 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     // Nesterov::new: prev coords = DB coordinates, prev grads = 0 (src/nesterov.rs:15-24)
     CK(upload(c.prev_x, d->x, sizeof(float) * N, c.stream));
     CK(upload(c.prev_y, d->y, sizeof(float) * N, c.stream));
-    for (float *a : {c.prev_gx, c.prev_gy, c.wlgx, c.wlgy, c.dgx, c.dgy})
+    for (float *a : {c.prev_gx, c.prev_gy, c.wlgx, c.wlgy})
         CK(cudaMemsetAsync(a, 0, sizeof(float) * ((size_t)N + 4), c.stream));
+    CK(cudaMemsetAsync(c.dgp, 0, sizeof(float2) * ((size_t)NM + 4), c.stream));
+    CK(cudaMemsetAsync(c.pos, 0, sizeof(int32_t) * ((size_t)NM + 4), c.stream));
     CK(upload(c.slot_cell, hslot_cell.data(), sizeof(int32_t) * P, c.stream));
     CK(upload(c.slot_off, hslot_off.data(), sizeof(float2) * P, c.stream));
     CK(cudaMemsetAsync(c.slot_grad, 0, sizeof(float2) * (P ? P : 1), c.stream));
@@ -843,8 +847,22 @@ extern "C" erp_status erp_get_array(erp_ctx *ctx, erp_array which, void *dst, si
     switch (which) {
     case ERP_ARR_WL_GRAD_X: src = c.wlgx; need = sizeof(float) * c.N; break;
     case ERP_ARR_WL_GRAD_Y: src = c.wlgy; need = sizeof(float) * c.N; break;
-    case ERP_ARR_DENS_GRAD_X: src = c.dgx; need = sizeof(float) * c.N; break;
-    case ERP_ARR_DENS_GRAD_Y: src = c.dgy; need = sizeof(float) * c.N; break;
+    case ERP_ARR_DENS_GRAD_X:
+    case ERP_ARR_DENS_GRAD_Y: {   // kept in scatter order on the device: back to cell order
+        need = sizeof(float) * c.N;
+        if (bytes < need) { c.err = "destination too small"; return ERP_EINVAL; }
+        std::vector<float2> g(c.NM ? c.NM : 1);
+        std::vector<int32_t> at(c.NM ? c.NM : 1);
+        CK(cudaMemcpyAsync(g.data(), c.dgp, sizeof(float2) * c.NM, cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaMemcpyAsync(at.data(), c.pos, sizeof(int32_t) * c.NM, cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+        float *o = (float *)dst;
+        for (int i = 0; i < c.N; ++i) {
+            const float2 v = i < c.NM ? g[at[i]] : make_float2(0.0f, 0.0f);
+            o[i] = which == ERP_ARR_DENS_GRAD_X ? v.x : v.y;
+        }
+        return ERP_OK;
+    }
     case ERP_ARR_DENSITY_I64: src = c.dmap; need = sizeof(int64_t) * mn; break;
     case ERP_ARR_DENSITY: src = c.rho; need = sizeof(float) * mn; break;
     case ERP_ARR_INITIAL: src = c.initial; need = sizeof(float) * mn; break;
@@ -1499,10 +1517,11 @@ extern "C" erp_status erp_estimate_footprint(const erp_design *d, const erp_para
     int64_t movable_pins = 0;
     if (d->inst_pin_ptr) movable_pins = d->inst_pin_ptr[NM];
     auto al = [](int64_t v) { return (v + 511) & ~int64_t(511); };   // allocation granularity
-    int64_t b = 18 * al(4 * (N + 4));
+    int64_t b = 16 * al(4 * (N + 4));
     b += al(4 * P) + 2 * al(8 * P) + al(4 * (E + 1)) + al(4 * E) + al(4 * (NM + 1)) + al(4 * movable_pins);
     b += al(8 * mn) + 9 * al(4 * mn) + al(8 * (int64_t)kMaxPartials) + al(sizeof(DevState));
     b += 5 * al(4 * (int64_t)NM) + al(16 * (int64_t)NM) + 2 * al(4 * (int64_t)scatter_tiles(m, n));   // scatter order
+    b += al(4 * (NM + 4)) + al(8 * (NM + 4));   // its inverse, the density gradient in that order
     b += al(8 * (m / 2)) + al(8 * (n / 2)) + al(8 * m) + al(8 * n) + al(4 * m) + al(4 * n);
     if (pp && pp->precision != ERP_PREC_FP32) {   // tensor-core plan: 4 transforms per axis + 7 map buffers
         const int64_t es = pp->precision == ERP_PREC_TF32_GEMM ? 4 : 4;   // fp32, or bf16 hi + lo

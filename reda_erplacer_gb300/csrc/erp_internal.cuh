@@ -90,7 +90,7 @@ struct Ctx {
     // --- cells [N] ---
     float *x, *y, *w, *h, *npins, *cw, *ch, *offx, *offy, *ratio;
     float2 *xy;                // (x, y) interleaved: one 8-byte gather per pin in the wirelength pass
-    float *wlgx, *wlgy, *dgx, *dgy;
+    float *wlgx, *wlgy;
     float *prev_x, *prev_y, *prev_gx, *prev_gy;
     // --- pins in internal slot order [NS] ---
     int32_t *slot_cell;
@@ -103,6 +103,8 @@ struct Ctx {
     int32_t *cell_slots;
     // --- scatter order [NM] (k_density_scatter; refreshed every kSortEvery steps) ---
     int32_t *perm, *skey;      // cell at each scatter position, its sort tile
+    int32_t *pos;              // scatter position of each movable cell (perm's inverse)
+    float2 *dgp;               // density gradient in scatter order (k_force writes it coalesced)
     float4 *soff;              // offx, offy, cw, ch in scatter order
     float *sratio;
     int32_t *sort_key, *sort_rank, *sort_hist, *sort_start;   // counting-sort scratch ([NM], [NM], tiles, tiles)

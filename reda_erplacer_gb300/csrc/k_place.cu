@@ -606,12 +606,13 @@ __global__ void __launch_bounds__(kThreads) k_sort_place(int NM, const int32_t *
                                                          const float *__restrict__ offy,
                                                          const float *__restrict__ cw, const float *__restrict__ ch,
                                                          const float *__restrict__ ratio, int32_t *__restrict__ perm,
-                                                         float4 *__restrict__ soff, float *__restrict__ sratio,
-                                                         int32_t *__restrict__ skey) {
+                                                         int32_t *__restrict__ pos, float4 *__restrict__ soff,
+                                                         float *__restrict__ sratio, int32_t *__restrict__ skey) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
         const int k = key[i];
         const int p = start[k] + rank[i];
         perm[p] = i;
+        pos[i] = p;
         soff[p] = make_float4(offx[i], offy[i], cw[i], ch[i]);
         sratio[p] = ratio[i];
         skey[p] = k;
@@ -685,13 +686,13 @@ __global__ void __launch_bounds__(kThreads) k_force(
     const float *__restrict__ sratio, const float *__restrict__ offx, const float *__restrict__ offy,
     const float *__restrict__ cw, const float *__restrict__ ch, const float *__restrict__ ratio, int m, int n,
     float bw, float bh, float inv_bw, float inv_bh, const float *__restrict__ fx,
-    const float *__restrict__ fy, float *__restrict__ gx_out, float *__restrict__ gy_out,
+    const float *__restrict__ fy, float2 *__restrict__ dgp, const int32_t *__restrict__ pos,
     int rescale, const float *__restrict__ wlgx, const float *__restrict__ wlgy,
     double *__restrict__ partials, DevState *st) {
     __shared__ double shr[kThreads / 32];
     if (st->done) return;
     // the field gathered over cell i's bins (src/eforce.rs)
-    auto force = [&](int i, float nx, float ny, float sx, float sy, float r) {
+    auto force = [&](float nx, float ny, float sx, float sy, float r) -> float2 {
         const int xl = force_bin_lo((nx - 0.0f) * inv_bw, m);
         const int xh = force_bin_hi((nx + sx - 0.0f) * inv_bw, m);
         const int yl = force_bin_lo((ny - 0.0f) * inv_bh, n);
@@ -707,23 +708,26 @@ __global__ void __launch_bounds__(kThreads) k_force(
                 gy += area * __ldg(ry + hh);
             }
         }
-        gx_out[i] = -gx * r;
-        gy_out[i] = -gy * r;
+        return make_float2(-gx * r, -gy * r);
     };
     // Inside the step graph (rescale = 1) the iteration-0 density-weight rescale
     // (src/nesterov.rs:47-55) rides on this pass: the WA gradient is complete and
     // the density gradient is produced here, so no extra launch per step.  That
     // pass runs in cell order, so its sums have a fixed grouping; every
     // other pass takes the cells in the scatter order, where a block's cells
-    // share a tile and so share field lines (the outputs are per cell: the same
-    // in any order).
+    // share a tile and so share field lines.  The gradient is stored in scatter
+    // order, dgp[p], coalesced; the Nesterov pass reads it back through pos.
+    // (Stored at the cell's own index, two scattered 4-byte stores per cell
+    // once the cells have spread and the scatter order no longer follows the
+    // cell numbering: 30.4 us at iteration 300 against 25.9 us this way.)
     if (rescale && st->iteration == 0) {   // grid-uniform
         Df sa = df_zero(), sb = df_zero();
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
             const float2 q = xy[i];
-            force(i, q.x + offx[i], q.y + offy[i], cw[i], ch[i], ratio[i]);
+            const float2 g = force(q.x + offx[i], q.y + offy[i], cw[i], ch[i], ratio[i]);
+            dgp[pos[i]] = g;
             sa = df_add(df_add(sa, fabsf(wlgx[i])), fabsf(wlgy[i]));
-            sb = df_add(df_add(sb, fabsf(gx_out[i])), fabsf(gy_out[i]));   // written by this thread
+            sb = df_add(df_add(sb, fabsf(g.x)), fabsf(g.y));
         }
         Df vals[2];
         vals[0] = block_sum(sa, shr);
@@ -744,7 +748,7 @@ __global__ void __launch_bounds__(kThreads) k_force(
         const int i = perm[p];
         const float2 q = xy[i];
         const float4 o = soff[p];   // offx, offy, cw, ch of cell i
-        force(i, q.x + o.x, q.y + o.y, o.z, o.w, sratio[p]);
+        dgp[p] = force(q.x + o.x, q.y + o.y, o.z, o.w, sratio[p]);
     }
 }
 
@@ -770,8 +774,8 @@ __global__ void k_energy(size_t mn, const float *__restrict__ psi, const float *
 __global__ void __launch_bounds__(kThreads) k_dw_rescale(int NM, int iter_arg,
                                                          const float *__restrict__ wlgx,
                                                          const float *__restrict__ wlgy,
-                                                         const float *__restrict__ dgx,
-                                                         const float *__restrict__ dgy,
+                                                         const float2 *__restrict__ dgp,
+                                                         const int32_t *__restrict__ pos,
                                                          double *__restrict__ partials,
                                                          DevState *st) {
     __shared__ double shr[kThreads / 32];
@@ -781,7 +785,8 @@ __global__ void __launch_bounds__(kThreads) k_dw_rescale(int NM, int iter_arg,
     Df a = df_zero(), b = df_zero();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
         a = df_add(df_add(a, fabsf(wlgx[i])), fabsf(wlgy[i]));
-        b = df_add(df_add(b, fabsf(dgx[i])), fabsf(dgy[i]));
+        const float2 g = dgp[pos[i]];
+        b = df_add(df_add(b, fabsf(g.x)), fabsf(g.y));
     }
     Df vals[2];
     vals[0] = block_sum(a, shr);
@@ -843,7 +848,7 @@ __device__ __forceinline__ void nesterov_grad_cell(float wlx, float wly, float d
 
 __global__ void __launch_bounds__(kThreads) k_nesterov_grad(
     int NM, int iter_arg, const float *__restrict__ wlgx, const float *__restrict__ wlgy,
-    const float *__restrict__ dgx, const float *__restrict__ dgy, const float *__restrict__ w,
+    const float2 *__restrict__ dgp, const int32_t *__restrict__ pos, const float *__restrict__ w,
     const float *__restrict__ h, const float *__restrict__ npins, const float *__restrict__ x,
     const float *__restrict__ y, const float *__restrict__ px, const float *__restrict__ py,
     float *__restrict__ pgx, float *__restrict__ pgy, double *__restrict__ partials, DevState *st) {
@@ -853,7 +858,10 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_grad(
     float numf = 0.0f, denf = 0.0f;
     const int n4 = NM >> 2;
     for (int i4 = blockIdx.x * blockDim.x + threadIdx.x; i4 < n4; i4 += gridDim.x * blockDim.x) {
-        const Cell4 a = ld4(wlgx, i4), b = ld4(wlgy, i4), c = ld4(dgx, i4), d = ld4(dgy, i4);
+        const Cell4 a = ld4(wlgx, i4), b = ld4(wlgy, i4);
+        const int4 at = reinterpret_cast<const int4 *>(pos)[i4];
+        const float2 g0 = dgp[at.x], g1 = dgp[at.y], g2 = dgp[at.z], g3 = dgp[at.w];
+        const Cell4 c = {{g0.x, g1.x, g2.x, g3.x}}, d = {{g0.y, g1.y, g2.y, g3.y}};
         const Cell4 ww = ld4(w, i4), hh = ld4(h, i4), np = ld4(npins, i4);
         const Cell4 xx = ld4(x, i4), yy = ld4(y, i4), qx = ld4(px, i4), qy = ld4(py, i4);
         Cell4 gx = ld4w(pgx, i4), gy = ld4w(pgy, i4);
@@ -867,7 +875,8 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_grad(
     if (blockIdx.x == 0 && threadIdx.x < (NM & 3)) {   // tail cells
         const int i = (n4 << 2) + threadIdx.x;
         float gx = pgx[i], gy = pgy[i];
-        nesterov_grad_cell(wlgx[i], wlgy[i], dgx[i], dgy[i], w[i], h[i], npins[i], x[i], y[i], px[i],
+        const float2 g = dgp[pos[i]];
+        nesterov_grad_cell(wlgx[i], wlgy[i], g.x, g.y, w[i], h[i], npins[i], x[i], y[i], px[i],
                            py[i], gx, gy, dw, numf, denf);
         pgx[i] = gx;
         pgy[i] = gy;
@@ -1140,7 +1149,8 @@ void launch_scatter_order(Ctx &c, cudaStream_t s) {
         c.sort_hist);
     k_sort_scan<<<1, 1024, 0, s>>>(ntiles, c.sort_hist, c.sort_start);
     k_sort_place<<<grid_for(c.NM), kThreads, 0, s>>>(c.NM, c.sort_key, c.sort_rank, c.sort_start, c.offx, c.offy,
-                                                     c.cw, c.ch, c.ratio, c.perm, c.soff, c.sratio, c.skey);
+                                                     c.cw, c.ch, c.ratio, c.perm, c.pos, c.soff, c.sratio,
+                                                     c.skey);
 }
 
 void launch_initial_density(Ctx &c, const float *, const float *, const float *, const float *) {
@@ -1188,7 +1198,7 @@ static int fit(int need, const std::atomic<int> &resident_a) {
 void launch_force(Ctx &c, int rescale) {
     k_force<<<fit(grid_for(c.NM, 152 * 16), g_res_force), kThreads, 0, c.stream>>>(
                c.NM, c.perm, c.xy, c.soff, c.sratio, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w,
-               c.bin_h, c.inv_bw, c.inv_bh, c.fx, c.fy, c.dgx, c.dgy, rescale, c.wlgx, c.wlgy, c.partials, c.st);
+               c.bin_h, c.inv_bw, c.inv_bh, c.fx, c.fy, c.dgp, c.pos, rescale, c.wlgx, c.wlgy, c.partials, c.st);
 }
 
 void launch_energy(Ctx &c) {
@@ -1200,12 +1210,12 @@ void launch_energy(Ctx &c) {
 void launch_nesterov(Ctx &c, int iter_arg) {
     if (iter_arg >= 0) {   // stage entry point; in the step graph k_force does the rescale
         const int g = grid_for(c.NM);
-        k_dw_rescale<<<g, kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx, c.dgy,
+        k_dw_rescale<<<g, kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgp, c.pos,
                                                    c.partials, c.st);
     }
     const int g4 = grid_for((c.NM + 3) / 4);
-    k_nesterov_grad<<<fit(g4, g_res_grad), kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgx,
-               c.dgy, c.w, c.h, c.npins, c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.partials, c.st);
+    k_nesterov_grad<<<fit(g4, g_res_grad), kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgp,
+               c.pos, c.w, c.h, c.npins, c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.partials, c.st);
     k_nesterov_update<<<fit(g4, g_res_update), kThreads, 0, c.stream>>>(c.NM, c.w, c.h, c.die_w, c.die_h,
                c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.xy, c.st);
 }
