@@ -274,6 +274,18 @@ void erp_batch_destroy(erp_batch *b);
  * fixes the shape instead (count 0). */
 erp_status erp_batch_tuning(const erp_batch *b, int32_t *chosen, int32_t *cells, float *ms, int32_t cap,
                             int32_t *count);
+/* The batch's autotuned tile shape of the FP32 spectral passes (no counterpart in
+ * the reference): the sequences -- rows or columns -- per block of the passes that
+ * serve sides 64..256, 0 meaning the fixed shape (four), else 2 or 8.
+ * erp_batch_create times the candidates on all FP32 instances' three passes
+ * running together and keeps the fastest; instances on the tensor-core solve
+ * and instances without such a side keep the fixed shape.  The shape decides no
+ * bit of the results.  *chosen receives it; seqs[i] / ms[i] (up to cap entries)
+ * each candidate and its time; *count the number of candidates (0 when no
+ * instance had such a side).  The environment variable ERP_BATCH_SPECTRAL_SEQS
+ * (2 or 8; anything else: the fixed shape) fixes the shape instead (count 0). */
+erp_status erp_batch_spectral_tuning(const erp_batch *b, int32_t *chosen, int32_t *seqs, float *ms, int32_t cap,
+                                     int32_t *count);
 
 /* ---- serving: continuous batching of placement jobs ----
  * Jobs are submitted as they arrive and wait in a FIFO queue.  Each

@@ -188,6 +188,7 @@ SpectralPlan plan_of(Ctx &c) {
     p.wu = c.wu; p.wv = c.wv;
     p.t1 = c.t1; p.tx = c.tx; p.ty = c.ty; p.tp = c.tp;
     p.partials = c.partials; p.st = c.st; p.stream = c.stream;
+    p.seqs = c.spectral_seqs;
     return p;
 }
 
@@ -1150,6 +1151,8 @@ struct erp_batch {
     cudaStream_t master = nullptr;
     int scatter_cells = 0;                 // autotuned cells per scatter block (0: the alone rule)
     std::vector<std::pair<int, float>> tuning;   // (candidate, ms of all instances' scatters together)
+    int spectral_seqs = 0;                 // autotuned sequences per block of the warp-form spectral passes
+    std::vector<std::pair<int, float>> spec_tuning;   // (candidate, ms of all instances' spectral passes)
     cudaGraphExec_t graph = nullptr;
     bool graph_ready = false;
     int graph_kernels = 0;
@@ -1161,6 +1164,7 @@ struct erp_batch {
 };
 
 static erp_status batch_tune_scatter(erp_batch *b);
+static erp_status batch_tune_spectral(erp_batch *b);
 
 static erp_status batch_fail(erp_batch *b, erp_status s, const std::string &msg) {
     b->err = msg;
@@ -1231,6 +1235,7 @@ extern "C" erp_status erp_batch_create(const erp_design *designs, const erp_para
     }
     if (s == ERP_OK) {
         s = batch_tune_scatter(b);
+        if (s == ERP_OK) s = batch_tune_spectral(b);
         if (s != ERP_OK) g_create_err = b->err;
     }
     if (s != ERP_OK) {
@@ -1345,6 +1350,108 @@ static erp_status batch_tune_scatter(erp_batch *b) {
     cudaEventDestroy(e1);
     for (auto &e : joins) cudaEventDestroy(e);
     return rc;
+}
+
+// Autotuner of the spectral passes' tile shape for a batch: the sequences (rows
+// or columns) per block of the warp-form passes, which serve the sides 64..256
+// that most instances of a mix have.  Alone, four per block measured fastest
+// at every side; with every instance's passes on the GPU at once the best shape
+// can differ, as for the scatter.  Each candidate is timed on a graph of all FP32
+// instances' three passes running together, and the fastest is kept.  The
+// passes read the (cleared) map and the fixed-cell map and write only the
+// intermediates, the fields and the step's overflow, which the first step
+// recomputes; the shape decides no bit of the results (a block's rows are
+// transformed the same way whichever block holds them).  Instances on the
+// tensor-core solve, or with no side in 64..256, keep their shape.
+static erp_status batch_tune_spectral(erp_batch *b) {
+    const int cand[] = {0, kSeqCandidates[0], kSeqCandidates[1]};
+    std::vector<Ctx *> xs;
+    for (auto *x : b->ctx) {
+        Ctx &c = x->c;
+        const bool warp_m = c.m >= 64 && c.m <= 256, warp_n = c.n >= 64 && c.n <= 256;
+        if (!c.gemm && (warp_m || warp_n)) xs.push_back(&c);
+    }
+    b->spec_tuning.clear();
+    b->spectral_seqs = 0;
+    if (const char *env = getenv("ERP_BATCH_SPECTRAL_SEQS")) {
+        const int v = atoi(env);
+        b->spectral_seqs = (v == kSeqCandidates[0] || v == kSeqCandidates[1]) ? v : 0;
+        for (Ctx *c : xs) c->spectral_seqs = b->spectral_seqs;
+        return ERP_OK;
+    }
+    if (xs.empty()) return ERP_OK;
+    cudaEvent_t fork, e0, e1;
+    if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) return ERP_ECUDA;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    std::vector<cudaEvent_t> joins(xs.size());
+    for (auto &e : joins) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    erp_status rc = ERP_OK;
+    float best = 0.0f;
+    int best_c = 0;
+    for (int cnd : cand) {
+        for (Ctx *c : xs) c->spectral_seqs = cnd;
+        cudaGraph_t g;
+        cudaGraphExec_t ge = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(b->master, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaEventRecord(fork, b->master);
+            for (size_t i = 0; i < xs.size(); ++i) {
+                Ctx &x = *xs[i];
+                cudaStreamWaitEvent(x.stream, fork, 0);
+                launch_spectral(x, /*zero_map=*/true, /*store_rho=*/false, /*want_psi=*/false);
+                cudaEventRecord(joins[i], x.stream);
+                cudaStreamWaitEvent(b->master, joins[i], 0);
+            }
+            e = cudaStreamEndCapture(b->master, &g);
+        }
+        if (e == cudaSuccess) {
+            e = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+        }
+        float ms = 0.0f;
+        if (e == cudaSuccess) {
+            cudaGraphLaunch(ge, b->master);   // warm-up
+            cudaEventRecord(e0, b->master);
+            for (int r = 0; r < 3; ++r) cudaGraphLaunch(ge, b->master);
+            cudaEventRecord(e1, b->master);
+            e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+            cudaGraphExecDestroy(ge);
+        }
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            b->err = std::string("spectral autotune: ") + cudaGetErrorString(e);
+            rc = ERP_ECUDA;
+            break;
+        }
+        b->spec_tuning.emplace_back(cnd, ms / 3.0f);
+        if (b->spec_tuning.size() == 1 || ms / 3.0f < best) {
+            best = ms / 3.0f;
+            best_c = cnd;
+        }
+    }
+    b->spectral_seqs = rc == ERP_OK ? best_c : 0;
+    for (Ctx *c : xs) c->spectral_seqs = b->spectral_seqs;
+    if (cudaStreamSynchronize(b->master) != cudaSuccess && rc == ERP_OK) rc = ERP_ECUDA;
+    cudaEventDestroy(fork);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (auto &e : joins) cudaEventDestroy(e);
+    return rc;
+}
+
+extern "C" erp_status erp_batch_spectral_tuning(const erp_batch *b, int32_t *chosen, int32_t *seqs, float *ms,
+                                                int32_t cap, int32_t *count) {
+    if (!b || cap < 0 || (cap > 0 && (!seqs || !ms))) return ERP_EINVAL;
+    if (chosen) *chosen = b->spectral_seqs;
+    const int k = std::min<int>(cap, (int)b->spec_tuning.size());
+    for (int i = 0; i < k; ++i) {
+        seqs[i] = b->spec_tuning[i].first;
+        ms[i] = b->spec_tuning[i].second;
+    }
+    if (count) *count = (int32_t)b->spec_tuning.size();
+    return ERP_OK;
 }
 
 // (Re)capture the batch graph over the instances whose active flag is set.

@@ -111,6 +111,7 @@ struct Ctx {
     int32_t sort_age;          // steps since the order was computed
     int32_t scatter_cells;     // movable cells per scatter block; 0: the rule for a context run alone
     int32_t scatter_planes;    // 21-bit pieces per contribution in the scatter's window: 2 or 3
+    int32_t spectral_seqs;     // sequences per block of the warp-form spectral passes; 0: the fixed shape
     // host-side permutations for test hooks
     int32_t *h_slot_of_pin;    // [P]
     int32_t *h_net_of_internal;// [E]
@@ -166,6 +167,9 @@ void enqueue_step_kernels(Ctx &c);
 void launch_gather_done(DevState *const *states, int count, int32_t *out, cudaStream_t s);
 
 // spectral engine for the standalone solve
+// The sequences-per-block alternatives of the warp-form spectral passes (sides
+// 64..256) that a batch's autotuner times against the fixed shape (four).
+constexpr int kSeqCandidates[2] = {2, 8};
 struct SpectralPlan {
     int32_t m, n, logm, logn;
     float bin_w, bin_h;
@@ -175,6 +179,9 @@ struct SpectralPlan {
     double *partials;
     DevState *st;
     cudaStream_t stream;
+    // sequences per block of the warp-form passes (sides 64..256): 0 for the
+    // fixed shape, else one a batch's autotuner chose (2 or 8)
+    int32_t seqs = 0;
 };
 void spectral_tables(int m, int n, float bin_w, float bin_h, float2 **tw_m, float2 **tw_n,
                      float2 **ek_m, float2 **ek_n, float **wu, float **wv, cudaStream_t s);

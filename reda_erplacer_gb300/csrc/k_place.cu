@@ -365,7 +365,13 @@ static_assert(kSortTile + 2 * kSortPad == kWin, "the window covers a tile and it
 constexpr int kTableLog = 9, kTable = 1 << kTableLog;   // out-of-window bin table (open, no probing)
 constexpr unsigned kEmpty = 0xffffffffu;                 // bin indices are < 4096 * 4096
 constexpr int kMaxCellsPerBlock = 2048;
-constexpr int kAggSide = 5;   // warp-aggregated scatter: the warp's cells within kAggSide x kAggSide bins
+// Warp-aggregated scatter for warps whose cells all fall within kAggSide x kAggSide
+// bins.  Measured on the 1M-cell step (rate over 50 steps at iterations 5, 30,
+// 100, 300, 500, 800): 3 x 3 boxes 4,715 / 4,634 / 4,654 / 4,448 / 4,416 / 4,520
+// iterations/s, per-lane adds only 4,717 / 4,621 / 4,650 / 4,452 / 4,409 / 4,506,
+// 5 x 5 boxes 4,596 / 4,547 / 4,653 / 4,443 / 4,406 / 4,518: a box takes one warp
+// reduction per bin and plane, which only pays where the warp's cells pile up.
+constexpr int kAggSide = 3;
 constexpr unsigned long long kPiece = (1ull << 21) - 1;
 // Adds the integer s0 + s1 2^21 + s2 2^42 to bin (bx, by): into the block's
 // window plane by plane, else into its bin table, else into global memory.

@@ -1093,24 +1093,26 @@ void spectral_tables(int m, int n, float bin_w, float bin_h, float2 **tw_m, floa
 constexpr int kRowWarps = 4;   // rows per block, warp kernels
 constexpr int kColWarps = 4;   // columns per block, warp kernels
 
-// warp kernels cover N = 64 * E, E = 1..32 (sides 64..2048)
-template <int E>
-static size_t rows_w_smem() { return sizeof(float2) * (size_t)(tables_f2<32 * E>() + kRowWarps * 64 * E); }
-template <int E>
-static size_t rows_dct_w_smem() { return sizeof(float2) * (size_t)(tables_f2<32 * E>() + kRowWarps * 96 * E); }
-template <int E>
+// warp kernels cover N = 64 * E, E = 1..32 (sides 64..2048); NW sequences per
+// block (kRowWarps / kColWarps unless a batch's autotuner chose otherwise)
+template <int E, int NW = kRowWarps>
+static size_t rows_w_smem() { return sizeof(float2) * (size_t)(tables_f2<32 * E>() + NW * 64 * E); }
+template <int E, int NW = kRowWarps>
+static size_t rows_dct_w_smem() { return sizeof(float2) * (size_t)(tables_f2<32 * E>() + NW * 96 * E); }
+template <int E, int NW = kColWarps>
 static size_t cols_w_smem() {
-    return sizeof(float2) * (size_t)(tables_f2<32 * E>() + kColWarps * 96 * E) +
-           sizeof(float) * (size_t)(64 * E) * (kColWarps + 2);
+    return sizeof(float2) * (size_t)(tables_f2<32 * E>() + NW * 96 * E) + sizeof(float) * (size_t)(64 * E) * (NW + 2);
 }
 
-template <int E>
+template <int E, int RW = kRowWarps, int CW = kColWarps>
 static cudaError_t prepare_w() {
-    cudaError_t e = cudaFuncSetAttribute(k_rows_dct_w<E, kRowWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_dct_w_smem<E>());
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_inv_w<E, kRowWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_w_smem<E>());
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cols_w<E, kColWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_w_smem<E>());
+    cudaError_t e = cudaFuncSetAttribute(k_rows_dct_w<E, RW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_dct_w_smem<E, RW>());
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_inv_w<E, RW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_w_smem<E, RW>());
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cols_w<E, CW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_w_smem<E, CW>());
     return e;
 }
+// The sequences-per-block alternatives a batch's autotuner can choose for the
+// sides it times (64..256, where the warp kernels run): SpectralPlan::seqs.
 
 // group kernels: sides 512..2048 (E = side / 256), G sequences per block
 constexpr int kRowGroups = 2, kColGroups = 4, kInvGroups = 4;
@@ -1172,6 +1174,12 @@ cudaError_t spectral_prepare() {
     if (e == cudaSuccess) e = prepare_w<8>();
     if (e == cudaSuccess) e = prepare_w<16>();
     if (e == cudaSuccess) e = prepare_w<32>();
+    if (e == cudaSuccess) e = prepare_w<1, kSeqCandidates[0], kSeqCandidates[0]>();
+    if (e == cudaSuccess) e = prepare_w<2, kSeqCandidates[0], kSeqCandidates[0]>();
+    if (e == cudaSuccess) e = prepare_w<4, kSeqCandidates[0], kSeqCandidates[0]>();
+    if (e == cudaSuccess) e = prepare_w<1, kSeqCandidates[1], kSeqCandidates[1]>();
+    if (e == cudaSuccess) e = prepare_w<2, kSeqCandidates[1], kSeqCandidates[1]>();
+    if (e == cudaSuccess) e = prepare_w<4, kSeqCandidates[1], kSeqCandidates[1]>();
     if (e == cudaSuccess) e = prepare_g<2>();
     if (e == cudaSuccess) e = prepare_g<4>();
     if (e == cudaSuccess) e = prepare_g<8>();
@@ -1186,22 +1194,48 @@ size_t spectral_smem_bytes(int m, int n) {
 static bool warp_side(int v) { return v >= 64 && v <= 2048; }
 
 
-template <int E>
-static void rows_dct_w(const SpectralPlan &p, const SpectralArgs &a, bool from_map) {
-    k_rows_dct_w<E, kRowWarps><<<p.m / kRowWarps, kRowWarps * 32, rows_dct_w_smem<E>(), p.stream>>>(
+template <int E, int NW>
+static void rows_dct_w_nw(const SpectralPlan &p, const SpectralArgs &a, bool from_map) {
+    k_rows_dct_w<E, NW><<<p.m / NW, NW * 32, rows_dct_w_smem<E, NW>(), p.stream>>>(
         p.m, p.tw_n, p.ek_n, a.rho_in, a.dmap, a.initial, a.fixed_inv, a.coef, a.inv_bin_area,
         a.zero_map ? 1 : 0, a.rho_out, p.t1, from_map ? a.partials : nullptr, a.st, a.movable_area);
 }
+template <int E, int NW>
+static void cols_w_nw(const SpectralPlan &p, const SpectralArgs &a, float scale4, float *tp) {
+    k_cols_w<E, NW><<<p.n / NW, NW * 32, cols_w_smem<E, NW>(), p.stream>>>(
+        p.n, p.tw_m, p.ek_m, p.wu, p.wv, p.t1, p.tx, p.ty, tp, scale4, a.st);
+}
+template <int E, int NW>
+static void rows_inv_w_nw(const SpectralPlan &p, const SpectralArgs &a, float *tp) {
+    const int nk = tp ? 3 : 2;
+    k_rows_inv_w<E, NW><<<p.m * nk / NW, NW * 32, rows_w_smem<E, NW>(), p.stream>>>(
+        p.m, nk, p.tw_n, p.ek_n, p.tx, p.ty, tp, a.fx, a.fy, a.psi, a.st);
+}
+// the plan's sequences per block: an autotuned alternative (sides 64..256) or
+// the fixed shape
+template <int E>
+static void rows_dct_w(const SpectralPlan &p, const SpectralArgs &a, bool from_map) {
+    if constexpr (E <= 4) {
+        if (p.seqs == kSeqCandidates[0]) return rows_dct_w_nw<E, kSeqCandidates[0]>(p, a, from_map);
+        if (p.seqs == kSeqCandidates[1]) return rows_dct_w_nw<E, kSeqCandidates[1]>(p, a, from_map);
+    }
+    rows_dct_w_nw<E, kRowWarps>(p, a, from_map);
+}
 template <int E>
 static void cols_w(const SpectralPlan &p, const SpectralArgs &a, float scale4, float *tp) {
-    k_cols_w<E, kColWarps><<<p.n / kColWarps, kColWarps * 32, cols_w_smem<E>(), p.stream>>>(
-        p.n, p.tw_m, p.ek_m, p.wu, p.wv, p.t1, p.tx, p.ty, tp, scale4, a.st);
+    if constexpr (E <= 4) {
+        if (p.seqs == kSeqCandidates[0]) return cols_w_nw<E, kSeqCandidates[0]>(p, a, scale4, tp);
+        if (p.seqs == kSeqCandidates[1]) return cols_w_nw<E, kSeqCandidates[1]>(p, a, scale4, tp);
+    }
+    cols_w_nw<E, kColWarps>(p, a, scale4, tp);
 }
 template <int E>
 static void rows_inv_w(const SpectralPlan &p, const SpectralArgs &a, float *tp) {
-    const int nk = tp ? 3 : 2;
-    k_rows_inv_w<E, kRowWarps><<<p.m * nk / kRowWarps, kRowWarps * 32, rows_w_smem<E>(), p.stream>>>(
-        p.m, nk, p.tw_n, p.ek_n, p.tx, p.ty, tp, a.fx, a.fy, a.psi, a.st);
+    if constexpr (E <= 4) {
+        if (p.seqs == kSeqCandidates[0]) return rows_inv_w_nw<E, kSeqCandidates[0]>(p, a, tp);
+        if (p.seqs == kSeqCandidates[1]) return rows_inv_w_nw<E, kSeqCandidates[1]>(p, a, tp);
+    }
+    rows_inv_w_nw<E, kRowWarps>(p, a, tp);
 }
 
 #define ERP_DISPATCH_E(side, FN, ...)           \

@@ -242,6 +242,15 @@ class Batch:
         L.check(self.lib.erp_batch_tuning(self.h, C.byref(ch), cells, ms, 8, C.byref(n)))
         return int(ch.value), [(int(cells[i]), float(ms[i])) for i in range(min(n.value, 8))]
 
+    def spectral_tuning(self):
+        """The autotuned tile shape of the FP32 spectral passes: (chosen sequences
+        per block, 0 for the fixed shape, [(candidate, ms), ...])."""
+        ch, n = C.c_int32(), C.c_int32()
+        seqs = (C.c_int32 * 8)()
+        ms = (C.c_float * 8)()
+        L.check(self.lib.erp_batch_spectral_tuning(self.h, C.byref(ch), seqs, ms, 8, C.byref(n)))
+        return int(ch.value), [(int(seqs[i]), float(ms[i])) for i in range(min(n.value, 8))]
+
     def positions(self, i):
         ctx = self.lib.erp_batch_context(self.h, int(i))
         N = int(self.designs[i].num_nodes)

@@ -246,23 +246,33 @@ def test_large_workload_shadowing(R, O):
 
 
 def test_large_workload_free_run(R, O):
-    """1,000,000 cells from the jittered start, 1,000 iterations, GPU against the
-    reference's FP32 rules: at the iteration where the GPU first reaches
-    overflow 0.10 and at the converged state, within the bar."""
+    """1,000,000 cells from the jittered start, 1,000 iterations, no reload: the
+    GPU against the reference's FP64 form and its FP32 rules at the iteration
+    where the GPU first reaches overflow 0.10 and at the converged state.
+
+    The FP32 rules are not deterministic past iteration 200: the bins take their
+    contributions by atomic adds in whatever order the threads reach them, as
+    the reference's Mutex-guarded bins do, and the loop amplifies the rounding.
+    Repeated runs of them put HPWL at the overflow-0.10 iteration anywhere in a
+    band about 0.6 % wide (985.2e6 to 990.8e6 in six runs, against the GPU's
+    990.7e6), so a single run of them is held to twice the bar; the FP64 form,
+    which is deterministic, is held to the bar itself."""
     d, cfg = R.workload_large()
     t0 = time.time()
     hg, og = gpu_trajectory(R, d, cfg, 1)
     hr, orf = oracle_trajectory(O, d, cfg, "reference_fp32", 1)
+    hf, of = oracle_trajectory(O, d, cfg, "fixed_fp64", 1)
     print(f"\n{time.time() - t0:.1f} s")
     kt = int(np.argmax(og <= 0.10))
     kg, hgc, ogc = converged(hg, og)
-    kr, hrc, orc = converged(hr, orf)
-    print(f"\noverflow 0.10 at iteration {kt + 1}: HPWL {hg[kt]:.6g} / {hr[kt]:.6g} "
-          f"({(hg[kt] - hr[kt]) / hr[kt]:+.2e}), overflow {og[kt]:.5f} / {orf[kt]:.5f}")
-    print(f"overflow minimum GPU {ogc:.5f} at {kg + 1} (HPWL {hgc:.6g}), reference {orc:.5f} at {kr + 1} "
-          f"(HPWL {hrc:.6g}); final HPWL {hg[-1]:.6g} / {hr[-1]:.6g}, overflow {og[-1]:.5f} / {orf[-1]:.5f}")
+    for name, h, o, bar in (("FP32 rules", hr, orf, 2 * HPWL_BAR), ("FP64 form", hf, of, HPWL_BAR)):
+        kr, hrc, orc = converged(h, o)
+        print(f"{name}: overflow 0.10 at iteration {kt + 1}: HPWL {hg[kt]:.6g} / {h[kt]:.6g} "
+              f"({(hg[kt] - h[kt]) / h[kt]:+.2e}), overflow {og[kt]:.5f} / {o[kt]:.5f}; overflow minimum GPU "
+              f"{ogc:.5f} at {kg + 1} (HPWL {hgc:.6g}), reference {orc:.5f} at {kr + 1} (HPWL {hrc:.6g}); "
+              f"final HPWL {hg[-1]:.6g} / {h[-1]:.6g}, overflow {og[-1]:.5f} / {o[-1]:.5f}")
+        assert abs(hg[kt] - h[kt]) / h[kt] <= bar, name
+        assert abs(og[kt] - o[kt]) <= OVF_BAR, name
+        assert abs(ogc - orc) <= OVF_BAR, name
+        assert abs(hgc - hrc) / hrc <= bar, name
     assert og[kt] <= 0.10
-    assert abs(hg[kt] - hr[kt]) / hr[kt] <= HPWL_BAR
-    assert abs(og[kt] - orf[kt]) <= OVF_BAR
-    assert abs(ogc - orc) <= OVF_BAR
-    assert abs(hgc - hrc) / hrc <= HPWL_BAR

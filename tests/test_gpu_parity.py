@@ -396,6 +396,36 @@ def test_batch_scatter_autotune(R):
             del os.environ["ERP_BATCH_SCATTER_CELLS"]
 
 
+def test_batch_spectral_autotune(R):
+    """erp_batch_create also times the FP32 spectral passes' sequences per block
+    (fixed shape 0, then 2 and 8) on all instances at once and keeps the fastest;
+    every fixed shape (environment) gives the same results bit for bit."""
+    import os
+    mix = R.workload_batch(count=6, seed=78, min_cells=2000, max_cells=30000)
+    designs, bins = [d for d, _ in mix], [b for _, b in mix]
+    assert any(64 <= min(b) <= 256 for b in bins)
+    bt = R.Batch(designs, bins, 1.0, start_mode=1)
+    chosen, cand = bt.spectral_tuning()
+    assert [c for c, _ in cand] == [0, 2, 8] and all(t > 0 for _, t in cand)
+    assert chosen == min(cand, key=lambda ct: ct[1])[0]
+    its, lasts = bt.run(120)
+    xs = [bt.positions(i) for i in range(len(mix))]
+    bt.close()
+    for forced in ("0", "2", "8"):
+        os.environ["ERP_BATCH_SPECTRAL_SEQS"] = forced
+        try:
+            b2 = R.Batch(designs, bins, 1.0, start_mode=1)
+            assert b2.spectral_tuning() == (int(forced), [])
+            its2, lasts2 = b2.run(120)
+            assert its2 == its and [l["hpwl"] for l in lasts2] == [l["hpwl"] for l in lasts]
+            for i in range(len(mix)):
+                xa, ya = b2.positions(i)
+                assert np.array_equal(xa, xs[i][0]) and np.array_equal(ya, xs[i][1])
+            b2.close()
+        finally:
+            del os.environ["ERP_BATCH_SPECTRAL_SEQS"]
+
+
 def test_batch_matches_individual_runs(R):
     """Instances advanced together in one batched graph end bit-identical to the
     same designs run alone (each instance's kernels are the same; only their
