@@ -199,12 +199,28 @@ __device__ __forceinline__ float wa_exact(const WaArgs &a, int net_begin, int ne
         float ex[D], enx[D], ey[D], eny[D];
         float s_xe = 0.f, s_xen = 0.f, s_e = 0.f, s_en = 0.f;
         float s_ye = 0.f, s_yen = 0.f, s_f = 0.f, s_fn = 0.f;
+        // Two pins bounded by themselves (no initial min / max): each pin is the
+        // maximum or the minimum, so of the eight exponentials six are exp(0) = 1
+        // and the other two are exp((min - max) / gamma), the very expressions the
+        // general form evaluates for those pins.
+        float e2x = 0.f, e2y = 0.f;
+        if (D == 2 && !general) {
+            e2x = expf((mnx - mxx) * inv_gamma);
+            e2y = expf((mny - mxy) * inv_gamma);
+        }
 #pragma unroll
         for (int q = 0; q < D; ++q) {
-            ex[q] = expf((px[q] - mxx) * inv_gamma);
-            enx[q] = expf((mnx - px[q]) * inv_gamma);
-            ey[q] = expf((py[q] - mxy) * inv_gamma);
-            eny[q] = expf((mny - py[q]) * inv_gamma);
+            if (D == 2 && !general) {
+                ex[q] = px[q] == mxx ? 1.0f : e2x;
+                enx[q] = px[q] == mnx ? 1.0f : e2x;
+                ey[q] = py[q] == mxy ? 1.0f : e2y;
+                eny[q] = py[q] == mny ? 1.0f : e2y;
+            } else {
+                ex[q] = expf((px[q] - mxx) * inv_gamma);
+                enx[q] = expf((mnx - px[q]) * inv_gamma);
+                ey[q] = expf((py[q] - mxy) * inv_gamma);
+                eny[q] = expf((mny - py[q]) * inv_gamma);
+            }
             s_xe = __fmaf_rn(px[q], ex[q], s_xe); s_xen = __fmaf_rn(px[q], enx[q], s_xen);
             s_e += ex[q]; s_en += enx[q];
             s_ye = __fmaf_rn(py[q], ey[q], s_ye); s_yen = __fmaf_rn(py[q], eny[q], s_yen);
