@@ -146,10 +146,11 @@ def test_nesterov_and_scheduler(case):
                  (s["gamma"], v.gamma))
         print(f"iteration {it}: displacement {ex:.2e} / {ey:.2e}; alpha, beta, density weight, gamma "
               f"{[abs(a - b) / abs(b) if b else abs(a) for a, b in pairs]}")
-        assert ex <= 1e-4 and ey <= 1e-4
+        # measured on the six designs: displacement <= 1.6e-6, scalars <= 1.1e-7
+        assert ex <= 1e-5 and ey <= 1e-5
         assert s["iteration"] == v.iteration
         for a, b in pairs:
-            assert abs(a - b) <= 1e-4 * abs(b) + 1e-12
+            assert abs(a - b) <= 1e-6 * abs(b) + 1e-12
         # keep both sides on identical positions for the next round
         o.set_positions(xg, yg)
 
@@ -490,8 +491,15 @@ def test_spectral_tensor_core_rejects_odd_sizes(R):
 def test_step_mixed_precision_forms(R, O, prec):
     """Placement step with the tensor-core spectral solve: the fixed-point map and
     rho are the FP32 path's bit for bit, the fields stay within the form's error,
-    and after 100 iterations overflow is within 0.005 and HPWL within 0.5 %
-    (BF16x3; TF32 within 2 %) of the plain FP32 run."""
+    and after 100 iterations overflow is within 0.005 and HPWL within 0.5 % of the
+    plain FP32 run for BF16x3, the mixed form that batching and serving use.
+
+    TF32 is held to 2 % HPWL: its operands keep 10 mantissa bits, the fields come
+    out about 2e-3 off the FP64 solve (stated by the benchmark's isolated-solve
+    section), and on this 20,000-cell design after 100 iterations from spread
+    positions its HPWL is 0.8 % from the FP32 run's.  It is an opt-in form with a
+    stated error, not one that meets the end-state bar here (on the 1M-cell
+    workload it lands 0.06 % from the FP32 run at iteration 444)."""
     d = small_synth(20000, seed=1, macros=0, io=400)
     xy = spread_positions(d, seed=5, frac=0.6)
     a = R.Placement(d, (256, 256), 1.0, start_mode=1)
@@ -511,7 +519,6 @@ def test_step_mixed_precision_forms(R, O, prec):
     ia, la = a.run(100, 0.0)
     ib, lb = b.run(100, 0.0)
     assert ia == ib == 100
-    # BF16x3 meets the 0.5 % HPWL bar; TF32 (10-bit operands) measured 0.8 % here
     assert abs(lb["hpwl"] - la["hpwl"]) <= (2e-2 if prec == 1 else 5e-3) * la["hpwl"]
     assert abs(lb["overflow"] - la["overflow"]) <= 5e-3
     a.close()
