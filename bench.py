@@ -277,7 +277,32 @@ def batch_section(args, device, world=1, rank=0):
     its, lasts = bt.run(args.batch_iters, stop_overflow=0.10)
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
+    packed_n = bt.packed_instances()
     bt.close()
+    # the same mix with a graph branch per instance instead of the packed launches,
+    # and a mix of many tiny instances (2,000-4,000 cells, 64^2 bins), where the
+    # launches rather than the work set the pace, in both forms
+    forms = {}
+    tiny = R.workload_batch(count=64 if world == 1 else 64 // world, seed=4100, min_cells=2000, max_cells=4000)
+    for name, jobs_ in (("mix", mix), ("tiny_mix", tiny)):
+        for form in ("packed", "branches"):
+            if name == "mix" and form == "packed":
+                forms["mix_packed_s"] = t_batch
+                continue
+            os.environ["ERP_BATCH_FORM"] = form
+            try:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                b2 = R.Batch([d for d, _ in jobs_], [b for _, b in jobs_], 1.0, start_mode=1, device=device)
+                b2.run(args.batch_iters, stop_overflow=0.10)
+                torch.cuda.synchronize()
+                forms[f"{name}_{form}_s"] = time.perf_counter() - t0
+                b2.close()
+            finally:
+                del os.environ["ERP_BATCH_FORM"]
+    forms = {k: allreduce_max(v, world) for k, v in forms.items()}
+    n_tiny = len(tiny) * world
+    del tiny
     seq_lat = []
     t0 = time.perf_counter()
     seq_its = []
@@ -330,6 +355,16 @@ def batch_section(args, device, world=1, rank=0):
                              "candidates_ms": {str(c): round(t, 4) for c, t in tune_ms},
                              "note": "0 = the rule of a context run alone; timed at creation, all instances' "
                                      "scatters together; included in batched_s"},
+        "packed_instances": packed_n,
+        "forms": {
+            "mix_packed_jobs_per_hour": K / forms["mix_packed_s"] * 3600.0,
+            "mix_branches_jobs_per_hour": K / forms["mix_branches_s"] * 3600.0,
+            "tiny_mix_instances": n_tiny,
+            "tiny_mix_packed_jobs_per_hour": n_tiny / forms["tiny_mix_packed_s"] * 3600.0,
+            "tiny_mix_branches_jobs_per_hour": n_tiny / forms["tiny_mix_branches_s"] * 3600.0,
+            "note": "packed: the FP32 instances with bins <= 256 advance in one launch per stage over a table of "
+                    "all of them; branches: a graph branch of ten kernels per instance. Same bits either way; "
+                    "times include context creation"},
         "spectral_autotune": {"seqs_per_block": spec_chosen,
                               "candidates_ms": {str(c): round(t, 4) for c, t in spec_ms},
                               "note": "rows / columns per block of the FP32 passes at sides 64-256 (0 = the "
@@ -542,7 +577,13 @@ def serve_section(args, device, world=1, rank=0):
     from reda_erplacer_gb300.serving import Server, run_stream
     specs = R.design.batch_specs(count=args.serve_jobs, seed=9000, min_cells=5000, max_cells=500000)
     pilot = [R.design.batch_job(*sp) for sp in specs[: min(32, len(specs))]]
-    bt = R.Batch([d for d, _ in pilot], [b for _, b in pilot], 1.0, start_mode=1, device=device)
+    # the server replays a graph per job, so its capacity is gauged with a batch
+    # of one branch per instance, not with the packed launches
+    os.environ["ERP_BATCH_FORM"] = "branches"
+    try:
+        bt = R.Batch([d for d, _ in pilot], [b for _, b in pilot], 1.0, start_mode=1, device=device)
+    finally:
+        del os.environ["ERP_BATCH_FORM"]
     t0 = time.perf_counter()
     bt.run(args.batch_iters, stop_overflow=0.10)
     cap = allreduce_sum(len(pilot) / (time.perf_counter() - t0), world)
@@ -861,6 +902,11 @@ def summary(line):
         out["batched_jobs_per_hour"] = round(b["jobs_per_hour_batched"])
         out["one_at_a_time_jobs_per_hour"] = round(b["jobs_per_hour_sequential"])
         out["batched_speedup"] = round(b["speedup"], 3)
+        f = b.get("forms")
+        if f:
+            out["batched_branches_jobs_per_hour"] = round(f["mix_branches_jobs_per_hour"])
+            out["tiny_mix_packed_jobs_per_hour"] = round(f["tiny_mix_packed_jobs_per_hour"])
+            out["tiny_mix_branches_jobs_per_hour"] = round(f["tiny_mix_branches_jobs_per_hour"])
         out["mixed_batched_speedup"] = round(b["mixed_batched"]["speedup_vs_fp32_one_at_a_time"], 3)
     sv = line.get("serving")
     if sv:

@@ -286,6 +286,17 @@ erp_status erp_batch_tuning(const erp_batch *b, int32_t *chosen, int32_t *cells,
  * (2 or 8; anything else: the fixed shape) fixes the shape instead (count 0). */
 erp_status erp_batch_spectral_tuning(const erp_batch *b, int32_t *chosen, int32_t *seqs, float *ms, int32_t cap,
                                      int32_t *count);
+/* How many of the batch's instances advance in packed launches (no counterpart
+ * in the reference): every FP32 instance whose bin grid is 64..256 on both axes
+ * (and that has movable cells and nets) runs each stage of its step inside one
+ * launch per stage and kernel variant that covers all such instances -- each
+ * block finds its instance in a packed table of their arguments -- instead of a
+ * graph branch of its own kernels; the rest keep a branch each.  The results are
+ * those of each instance run alone, bit for bit.  With fewer than four such
+ * instances every instance keeps a branch (count 0), and the same rule applies
+ * whenever retirements leave fewer than four active.  The environment variable
+ * ERP_BATCH_FORM=branches gives every instance a branch instead (count 0). */
+erp_status erp_batch_packed(const erp_batch *b, int32_t *packed_instances);
 
 /* ---- serving: continuous batching of placement jobs ----
  * Jobs are submitted as they arrive and wait in a FIFO queue.  Each

@@ -195,7 +195,7 @@ SpectralPlan plan_of(Ctx &c) {
 }  // namespace
 
 namespace erp {
-void launch_spectral(Ctx &c, bool zero_map, bool store_rho, bool want_psi) {
+static SpectralArgs spectral_args(Ctx &c, bool zero_map, bool store_rho, bool want_psi) {
     SpectralArgs a;
     a.dmap = c.dmap;
     a.initial = c.initial;
@@ -210,6 +210,11 @@ void launch_spectral(Ctx &c, bool zero_map, bool store_rho, bool want_psi) {
     a.psi = want_psi ? c.psi : nullptr;
     a.partials = c.partials;
     a.st = c.st;
+    return a;
+}
+
+void launch_spectral(Ctx &c, bool zero_map, bool store_rho, bool want_psi) {
+    const SpectralArgs a = spectral_args(c, zero_map, store_rho, want_psi);
     if (c.gemm) {   // tensor-core precisions: rho, then the contractions (rho_out is c.rho itself)
         launch_map_rho(a, (size_t)c.m * c.n, c.rho, c.stream);
         dctgemm_solve(*c.gemm, c.rho, c.fx, c.fy, a.psi, &c.st->status);
@@ -1152,6 +1157,10 @@ struct erp_batch {
     int scatter_cells = 0;                 // autotuned cells per scatter block (0: the alone rule)
     std::vector<std::pair<int, float>> tuning;   // (candidate, ms of all instances' scatters together)
     int spectral_seqs = 0;                 // autotuned sequences per block of the warp-form spectral passes
+    bool packed = true;                    // small FP32 instances in packed launches (else a branch each)
+    int packed_instances = 0;              // how many of them (at creation)
+    void *pack_dev = nullptr;              // argument tables of the packed launches
+    size_t pack_cap = 0;
     std::vector<std::pair<int, float>> spec_tuning;   // (candidate, ms of all instances' spectral passes)
     cudaGraphExec_t graph = nullptr;
     bool graph_ready = false;
@@ -1165,6 +1174,11 @@ struct erp_batch {
 
 static erp_status batch_tune_scatter(erp_batch *b);
 static erp_status batch_tune_spectral(erp_batch *b);
+static bool packable(const Ctx &c);
+// Packed launches pay once several instances share them: one tiny instance
+// alone ran 47.9 us per iteration in a branch against 53.5 packed, eight 73.6
+// against 63.6, sixty-four 710 against 151.
+constexpr int kPackMin = 4;
 
 static erp_status batch_fail(erp_batch *b, erp_status s, const std::string &msg) {
     b->err = msg;
@@ -1237,6 +1251,14 @@ extern "C" erp_status erp_batch_create(const erp_design *designs, const erp_para
         s = batch_tune_scatter(b);
         if (s == ERP_OK) s = batch_tune_spectral(b);
         if (s != ERP_OK) g_create_err = b->err;
+    }
+    if (s == ERP_OK) {
+        const char *form = getenv("ERP_BATCH_FORM");
+        b->packed = !(form && strcmp(form, "branches") == 0);
+        b->packed_instances = 0;
+        if (b->packed)
+            for (auto *x : b->ctx) b->packed_instances += packable(x->c) ? 1 : 0;
+        if (b->packed_instances < kPackMin) b->packed_instances = 0;
     }
     if (s != ERP_OK) {
         erp_batch_destroy(b);
@@ -1441,6 +1463,12 @@ static erp_status batch_tune_spectral(erp_batch *b) {
     return rc;
 }
 
+extern "C" erp_status erp_batch_packed(const erp_batch *b, int32_t *packed_instances) {
+    if (!b || !packed_instances) return ERP_EINVAL;
+    *packed_instances = b->packed_instances;
+    return ERP_OK;
+}
+
 extern "C" erp_status erp_batch_spectral_tuning(const erp_batch *b, int32_t *chosen, int32_t *seqs, float *ms,
                                                 int32_t cap, int32_t *count) {
     if (!b || cap < 0 || (cap > 0 && (!seqs || !ms))) return ERP_EINVAL;
@@ -1454,11 +1482,62 @@ extern "C" erp_status erp_batch_spectral_tuning(const erp_batch *b, int32_t *cho
     return ERP_OK;
 }
 
-// (Re)capture the batch graph over the instances whose active flag is set.
+// Whether an instance's step runs in the batch's packed launches: the FP32
+// solve in its warp forms (bins 64..256 on both axes), with movable cells and
+// nets.  Larger grids, whose kernels are long enough for their launches not to
+// matter, and the tensor-core solve keep a graph branch each.
+static bool packable(const Ctx &c) {
+    return !c.gemm && c.m >= 64 && c.m <= 256 && c.n >= 64 && c.n <= 256 && c.NM > 0 && c.E > 0;
+}
+
+// The packed launches of one step over xs, in stage order, with their argument
+// tables uploaded to the batch's device buffer.
+static erp_status batch_pack_plan(erp_batch *b, const std::vector<Ctx *> &xs, std::vector<PackedLaunch> &ls) {
+    PackedArena ar;
+    for (PackKind k : {PK_WA, PK_GATHER, PK_SCATTER}) packed_place_stage(k, xs, ar, ls);
+    std::vector<SpectralJob> jobs;
+    for (Ctx *c : xs) jobs.push_back(SpectralJob{plan_of(*c), spectral_args(*c, true, false, false)});
+    for (PackKind k : {PK_ROWS_DCT_W, PK_COLS_W, PK_ROWS_INV_W}) packed_spectral_stage(k, jobs, ar, ls);
+    for (PackKind k : {PK_FORCE, PK_GRAD, PK_UPDATE, PK_SCHED}) packed_place_stage(k, xs, ar, ls);
+    if (ar.host.size() > b->pack_cap) {
+        if (b->pack_dev) cudaFree(b->pack_dev);
+        b->pack_dev = nullptr;
+        b->pack_cap = 0;
+        if (cudaMalloc(&b->pack_dev, ar.host.size()) != cudaSuccess)
+            return batch_fail(b, ERP_ENOMEM, "packed argument tables: allocation failed");
+        b->pack_cap = ar.host.size();
+    }
+    if (!ar.host.empty() &&
+        cudaMemcpy(b->pack_dev, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return batch_fail(b, ERP_ECUDA, "packed argument tables: upload failed");
+    return ERP_OK;
+}
+
+// (Re)capture the batch graph over the instances whose active flag is set:
+// the packable ones as one chain of packed launches (one per stage and kernel
+// variant), every other one as a branch of its own kernels.
 static erp_status batch_graph(erp_batch *b, const std::vector<char> &active) {
     if (b->graph_ready) {
         cudaGraphExecDestroy(b->graph);
         b->graph_ready = false;
+    }
+    std::vector<Ctx *> xs;
+    std::vector<char> branch(b->ctx.size(), 0);
+    for (size_t i = 0; i < b->ctx.size(); ++i) {
+        if (!active[i]) continue;
+        Ctx &c = b->ctx[i]->c;
+        if (b->packed && packable(c)) xs.push_back(&c);
+        else branch[i] = 1;
+    }
+    if (xs.size() < (size_t)kPackMin) {   // too few to pay for the table lookups: branches
+        for (size_t i = 0; i < b->ctx.size(); ++i)
+            if (active[i]) branch[i] = 1;
+        xs.clear();
+    }
+    std::vector<PackedLaunch> ls;
+    if (!xs.empty()) {
+        erp_status ps = batch_pack_plan(b, xs, ls);
+        if (ps != ERP_OK) return ps;
     }
     cudaEvent_t fork;
     if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess)
@@ -1470,13 +1549,17 @@ static erp_status batch_graph(erp_batch *b, const std::vector<char> &active) {
     if (e == cudaSuccess) {
         cudaEventRecord(fork, b->master);
         for (size_t i = 0; i < b->ctx.size(); ++i) {
-            if (!active[i]) continue;
+            if (!branch[i]) continue;
             Ctx &c = b->ctx[i]->c;
             cudaStreamWaitEvent(c.stream, fork, 0);
             enqueue_step_kernels(c);
             cudaEventRecord(joins[i], c.stream);
-            cudaStreamWaitEvent(b->master, joins[i], 0);
         }
+        const unsigned char *dev = static_cast<const unsigned char *>(b->pack_dev);
+        for (const PackedLaunch &l : ls)
+            if (!packed_place_launch(l, dev, b->master)) packed_spectral_launch(l, dev, b->master);
+        for (size_t i = 0; i < b->ctx.size(); ++i)
+            if (branch[i]) cudaStreamWaitEvent(b->master, joins[i], 0);
         e = cudaStreamEndCapture(b->master, &g);
     }
     if (e == cudaSuccess) {
@@ -1611,6 +1694,7 @@ extern "C" void erp_batch_destroy(erp_batch *b) {
     if (b->d_states) cudaFree(b->d_states);
     if (b->d_done) cudaFree(b->d_done);
     if (b->h_done) cudaFreeHost(b->h_done);
+    if (b->pack_dev) cudaFree(b->pack_dev);
     delete b;
 }
 

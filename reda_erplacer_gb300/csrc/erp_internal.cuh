@@ -5,8 +5,10 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include <string>
+#include <vector>
 
 #include "erplacer.h"
 
@@ -166,6 +168,67 @@ void enqueue_step_kernels(Ctx &c);
 // Gather the retire flags of several contexts into out[i] (device pointers).
 void launch_gather_done(DevState *const *states, int count, int32_t *out, cudaStream_t s);
 
+// ---- packed launches (batches) ----
+// One grid over the blocks of many instances of one kernel: instance i owns
+// blocks [block0[i], block0[i + 1]) and reads its arguments from tab[i].  Each
+// instance's blocks see the block index and the grid size they would have in a
+// launch of their own, so every instance computes the same bits as alone.
+template <typename P>
+struct Packed {
+    const P *tab;
+    const int32_t *block0;
+    int32_t n;
+};
+// the instance that owns block b (block0 ascending, block0[0] = 0)
+__device__ __forceinline__ int packed_instance(const int32_t *__restrict__ block0, int n, int b) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(block0 + mid) <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+// The packed form of a kernel whose body is BODY(args, block, grid).
+template <typename P, void (*BODY)(const P &, int, int), int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_packed(const __grid_constant__ Packed<P> pk) {
+    const int b = (int)blockIdx.x;
+    const int i = packed_instance(pk.block0, pk.n, b);
+    const int b0 = pk.block0[i];
+    BODY(pk.tab[i], b - b0, pk.block0[i + 1] - b0);
+}
+// The argument tables of a batch's packed step, built on the host (one buffer,
+// copied once to one device buffer), and its launches in stage order.
+struct PackedArena {
+    std::vector<unsigned char> host;
+    size_t put(const void *p, size_t bytes) {
+        const size_t off = (host.size() + 255) & ~size_t(255);
+        host.resize(off + bytes);
+        if (bytes) memcpy(host.data() + off, p, bytes);
+        return off;
+    }
+};
+struct PackedLaunch {
+    int kind;        // PackKind
+    int variant;     // template variant of the kernel (scatter planes; spectral E and NW)
+    size_t tab, block0;   // offsets of the argument table and the block prefix in the arena
+    int n, blocks, threads;
+    size_t smem;
+};
+template <typename P>
+inline Packed<P> packed_args(const PackedLaunch &l, const unsigned char *dev) {
+    return Packed<P>{reinterpret_cast<const P *>(dev + l.tab), reinterpret_cast<const int32_t *>(dev + l.block0),
+                     l.n};
+}
+enum PackKind { PK_WA, PK_GATHER, PK_SCATTER, PK_ROWS_DCT_W, PK_COLS_W, PK_ROWS_INV_W, PK_FORCE, PK_GRAD, PK_UPDATE,
+                PK_SCHED };
+// Appends one packed launch of the given kind over the contexts xs (k_place.cu:
+// wirelength, gather, scatter, force, Nesterov, scheduler; the scatter one per
+// plane count in use), and issues a planned launch with the arena at dev (false:
+// not one of its kinds).
+void packed_place_stage(PackKind k, const std::vector<Ctx *> &xs, PackedArena &ar, std::vector<PackedLaunch> &out);
+bool packed_place_launch(const PackedLaunch &l, const unsigned char *dev, cudaStream_t s);
+
 // spectral engine for the standalone solve
 // The sequences-per-block alternatives of the warp-form spectral passes (sides
 // 64..256) that a batch's autotuner times against the fixed shape (four).
@@ -198,6 +261,16 @@ struct SpectralArgs {
     DevState *st = nullptr;
 };
 void launch_spectral_plan(const SpectralPlan &p, const SpectralArgs &a);
+// The warp-form passes (sides 64..256) of many solves as packed launches, one
+// per template variant in use (k_spectral.cu): kind PK_ROWS_DCT_W, PK_COLS_W or
+// PK_ROWS_INV_W.
+struct SpectralJob {
+    SpectralPlan p;
+    SpectralArgs a;
+};
+void packed_spectral_stage(PackKind k, const std::vector<SpectralJob> &v, PackedArena &ar,
+                           std::vector<PackedLaunch> &out);
+bool packed_spectral_launch(const PackedLaunch &l, const unsigned char *dev, cudaStream_t s);
 // the map -> rho conversion, overflow and zeroing of R1 alone (tensor-core precisions)
 void launch_map_rho(const SpectralArgs &a, size_t mn, float *rho, cudaStream_t s);
 cudaError_t spectral_prepare();

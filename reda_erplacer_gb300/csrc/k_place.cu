@@ -252,15 +252,26 @@ struct WaClasses {
     int block0[kNumClasses + 1];
 };
 
-__global__ void __launch_bounds__(kThreads, 4) k_wa(WaArgs a, WaClasses cl, float gamma_arg,
-                                                 double *__restrict__ partials, DevState *st) {
+struct WaP {
+    WaArgs a;
+    WaClasses cl;
+    float gamma_arg;
+    double * partials;
+    DevState * st;
+};
+__device__ __forceinline__ void wa_body(const WaP &p, int bid, int nblk) {
+    WaArgs a = p.a;
+    const WaClasses &cl = p.cl;
+    float gamma_arg = p.gamma_arg;
+    double *__restrict__ partials = p.partials;
+    DevState * st = p.st;
     __shared__ double shr[kThreads / 32];
     if (st->done) return;
     const float gamma = gamma_arg > 0.f ? gamma_arg : st->gamma;
     a.inv_gamma = 1.0f / gamma;                        // src/hpwl.rs:166
     // the large-degree classes (longest blocks) take the first block indices, so
     // they are dispatched first and the short blocks fill in behind them
-    const int vb = (int)gridDim.x - 1 - (int)blockIdx.x;
+    const int vb = (int)nblk - 1 - (int)bid;
     int k = 0;
     while (k + 1 < kNumClasses && vb >= cl.block0[k + 1]) ++k;
     const int cb = vb - cl.block0[k], cg = cl.block0[k + 1] - cl.block0[k];
@@ -282,8 +293,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_wa(WaArgs a, WaClasses cl, floa
     }
 #undef ERP_WA_EXACT
     const Df vals[1] = {block_sum(hp, shr)};
-    if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_HPWL], gridDim.x)) {
-        const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
+    if (arrive_last(partials, bid, 1, vals, &st->ctr[CTR_HPWL], nblk)) {
+        const double tot = sum_partials(partials, nblk, 1, 0, shr);
         if (threadIdx.x == 0) {
             st->hpwl = tot;
             st->hpwl_f = (float)tot;
@@ -291,6 +302,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_wa(WaArgs a, WaClasses cl, floa
         }
     }
 }
+__global__ void __launch_bounds__(kThreads, 4) k_wa(const __grid_constant__ WaP p) { wa_body(p, blockIdx.x, gridDim.x); }
+
 
 __global__ void k_wl_zero(DevState *st) {
     if (threadIdx.x == 0 && !st->done) {
@@ -303,13 +316,25 @@ __global__ void k_wl_zero(DevState *st) {
 // gradients in macro_2_pins order; movable instances only.  The slot indices of
 // up to four pins are loaded, then their gradients, then summed in list order:
 // two memory round trips per four pins instead of two per pin.
-__global__ void __launch_bounds__(kThreads) k_wl_gather(int NM, const int32_t *__restrict__ ptr,
-                                                        const int32_t *__restrict__ slots,
-                                                        const float2 *__restrict__ g,
-                                                        float *__restrict__ gx, float *__restrict__ gy,
-                                                        const DevState *__restrict__ st) {
+struct GatherP {
+    int NM;
+    const int32_t * ptr;
+    const int32_t * slots;
+    const float2 * g;
+    float * gx;
+    float * gy;
+    const DevState * st;
+};
+__device__ __forceinline__ void wl_gather_body(const GatherP &p, int bid, int nblk) {
+    int NM = p.NM;
+    const int32_t *__restrict__ ptr = p.ptr;
+    const int32_t *__restrict__ slots = p.slots;
+    const float2 *__restrict__ g = p.g;
+    float *__restrict__ gx = p.gx;
+    float *__restrict__ gy = p.gy;
+    const DevState *__restrict__ st = p.st;
     if (st->done) return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
+    for (int i = bid * blockDim.x + threadIdx.x; i < NM; i += nblk * blockDim.x) {
         float sx = 0.0f, sy = 0.0f;
         const int e = ptr[i + 1];
         for (int k0 = ptr[i]; k0 < e; k0 += 4) {
@@ -330,6 +355,8 @@ __global__ void __launch_bounds__(kThreads) k_wl_gather(int NM, const int32_t *_
         gy[i] = sy;
     }
 }
+__global__ void __launch_bounds__(kThreads) k_wl_gather(const __grid_constant__ GatherP p) { wl_gather_body(p, blockIdx.x, gridDim.x); }
+
 
 // ============================ density ============================
 // Bin coordinate limited to [-1, nbins] before the float->int conversion: the
@@ -434,12 +461,42 @@ __device__ __forceinline__ void scatter_add(int bx, int by, unsigned long long c
                         PLANES == 3 ? (unsigned)(c >> 42) : 0u, wox, woy, n, win, tkey, tplane, map);
 }
 
+struct ScatterP {
+    int NM;
+    const int32_t * perm;
+    const float2 * xy;
+    const float4 * soff;
+    const float * sratio;
+    const int32_t * skey;
+    int nty;
+    int m;
+    int n;
+    float bw;
+    float bh;
+    float inv_bw;
+    float inv_bh;
+    float scale;
+    unsigned long long * map;
+    const DevState * st;
+};
 template <int PLANES>
-__global__ void __launch_bounds__(kThreads) k_density_scatter(
-    int NM, const int32_t *__restrict__ perm, const float2 *__restrict__ xy, const float4 *__restrict__ soff,
-    const float *__restrict__ sratio, const int32_t *__restrict__ skey, int nty, int m, int n, float bw,
-    float bh, float inv_bw, float inv_bh, float scale, unsigned long long *__restrict__ map,
-    const DevState *__restrict__ st) {
+__device__ __forceinline__ void density_scatter_body(const ScatterP &p, int bid, int nblk) {
+    int NM = p.NM;
+    const int32_t *__restrict__ perm = p.perm;
+    const float2 *__restrict__ xy = p.xy;
+    const float4 *__restrict__ soff = p.soff;
+    const float *__restrict__ sratio = p.sratio;
+    const int32_t *__restrict__ skey = p.skey;
+    int nty = p.nty;
+    int m = p.m;
+    int n = p.n;
+    float bw = p.bw;
+    float bh = p.bh;
+    float inv_bw = p.inv_bw;
+    float inv_bh = p.inv_bh;
+    float scale = p.scale;
+    unsigned long long *__restrict__ map = p.map;
+    const DevState *__restrict__ st = p.st;
     extern __shared__ unsigned dsm[];
     unsigned *win = dsm;                                  // window planes: bits 0-20, 21-41 (, 42-62)
     unsigned *tkey = dsm + PLANES * kWin * kWin;          // bin table: keys (bin index or kEmpty)
@@ -451,8 +508,8 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
         for (int k = threadIdx.x; k < PLANES * kTable; k += blockDim.x) tplane[k] = 0u;
     }
     if (st->done) return;
-    const int per = ((NM + gridDim.x - 1) / gridDim.x + 31) & ~31;   // <= kMaxCellsPerBlock (launcher)
-    const int c0 = blockIdx.x * per, c1 = min(c0 + per, NM);
+    const int per = ((NM + nblk - 1) / nblk + 31) & ~31;   // <= kMaxCellsPerBlock (launcher)
+    const int c0 = bid * per, c1 = min(c0 + per, NM);
     int wox = 0, woy = 0;   // window origin: the sort tile of the block's first cell, less the pad
     if (c0 < NM) {
         const int k0 = skey[c0];
@@ -550,6 +607,9 @@ __global__ void __launch_bounds__(kThreads) k_density_scatter(
         if (v) atomicAdd(map + bin, v);
     }
 }
+template <int PLANES>
+__global__ void __launch_bounds__(kThreads) k_density_scatter(const __grid_constant__ ScatterP p) { density_scatter_body<PLANES>(p, blockIdx.x, gridDim.x); }
+
 
 size_t density_scatter_smem(int planes) { return sizeof(unsigned) * (planes * kWin * kWin + (planes + 1) * kTable); }
 
@@ -643,12 +703,15 @@ __global__ void __launch_bounds__(kThreads) k_sort_place(int NM, const int32_t *
 
 int scatter_tiles(int m, int n) { return ((m + kSortTile - 1) / kSortTile) * ((n + kSortTile - 1) / kSortTile); }
 
+static cudaError_t packed_prepare();
 cudaError_t place_prepare() {
     cudaError_t e = cudaFuncSetAttribute(k_density_scatter<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)density_scatter_smem(2));
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_density_scatter<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)density_scatter_smem(3));
+    e = cudaFuncSetAttribute(k_density_scatter<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)density_scatter_smem(3));
+    if (e != cudaSuccess) return e;
+    return packed_prepare();
 }
 
 // compute_density_overflow (src/density.rs:16-23): overlap through bin centres
@@ -703,14 +766,59 @@ __device__ __forceinline__ float tri_raw(float x, float s, int k, float bs) {
 }
 
 // compute_electric_force (src/eforce.rs:15-91)
-__global__ void __launch_bounds__(kThreads) k_force(
-    int NM, const int32_t *__restrict__ perm, const float2 *__restrict__ xy, const float4 *__restrict__ soff,
-    const float *__restrict__ sratio, const float *__restrict__ offx, const float *__restrict__ offy,
-    const float *__restrict__ cw, const float *__restrict__ ch, const float *__restrict__ ratio, int m, int n,
-    float bw, float bh, float inv_bw, float inv_bh, const float *__restrict__ fx,
-    const float *__restrict__ fy, float2 *__restrict__ dgp, const int32_t *__restrict__ pos,
-    int rescale, const float *__restrict__ wlgx, const float *__restrict__ wlgy,
-    double *__restrict__ partials, DevState *st) {
+struct ForceP {
+    int NM;
+    const int32_t * perm;
+    const float2 * xy;
+    const float4 * soff;
+    const float * sratio;
+    const float * offx;
+    const float * offy;
+    const float * cw;
+    const float * ch;
+    const float * ratio;
+    int m;
+    int n;
+    float bw;
+    float bh;
+    float inv_bw;
+    float inv_bh;
+    const float * fx;
+    const float * fy;
+    float2 * dgp;
+    const int32_t * pos;
+    int rescale;
+    const float * wlgx;
+    const float * wlgy;
+    double * partials;
+    DevState * st;
+};
+__device__ __forceinline__ void force_body(const ForceP &p, int bid, int nblk) {
+    int NM = p.NM;
+    const int32_t *__restrict__ perm = p.perm;
+    const float2 *__restrict__ xy = p.xy;
+    const float4 *__restrict__ soff = p.soff;
+    const float *__restrict__ sratio = p.sratio;
+    const float *__restrict__ offx = p.offx;
+    const float *__restrict__ offy = p.offy;
+    const float *__restrict__ cw = p.cw;
+    const float *__restrict__ ch = p.ch;
+    const float *__restrict__ ratio = p.ratio;
+    int m = p.m;
+    int n = p.n;
+    float bw = p.bw;
+    float bh = p.bh;
+    float inv_bw = p.inv_bw;
+    float inv_bh = p.inv_bh;
+    const float *__restrict__ fx = p.fx;
+    const float *__restrict__ fy = p.fy;
+    float2 *__restrict__ dgp = p.dgp;
+    const int32_t *__restrict__ pos = p.pos;
+    int rescale = p.rescale;
+    const float *__restrict__ wlgx = p.wlgx;
+    const float *__restrict__ wlgy = p.wlgy;
+    double *__restrict__ partials = p.partials;
+    DevState * st = p.st;
     __shared__ double shr[kThreads / 32];
     if (st->done) return;
     // the field gathered over cell i's bins (src/eforce.rs)
@@ -744,7 +852,7 @@ __global__ void __launch_bounds__(kThreads) k_force(
     // cell numbering: 30.4 us at iteration 300 against 25.9 us this way.)
     if (rescale && st->iteration == 0) {   // grid-uniform
         Df sa = df_zero(), sb = df_zero();
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NM; i += gridDim.x * blockDim.x) {
+        for (int i = bid * blockDim.x + threadIdx.x; i < NM; i += nblk * blockDim.x) {
             const float2 q = xy[i];
             const float2 g = force(q.x + offx[i], q.y + offy[i], cw[i], ch[i], ratio[i]);
             dgp[pos[i]] = g;
@@ -754,9 +862,9 @@ __global__ void __launch_bounds__(kThreads) k_force(
         Df vals[2];
         vals[0] = block_sum(sa, shr);
         vals[1] = block_sum(sb, shr);
-        if (arrive_last(partials, blockIdx.x, 2, vals, &st->ctr[CTR_ABS], gridDim.x)) {
-            const double num = sum_partials(partials, gridDim.x, 2, 0, shr);
-            const double den = sum_partials(partials, gridDim.x, 2, 1, shr);
+        if (arrive_last(partials, bid, 2, vals, &st->ctr[CTR_ABS], nblk)) {
+            const double num = sum_partials(partials, nblk, 2, 0, shr);
+            const double den = sum_partials(partials, nblk, 2, 1, shr);
             if (threadIdx.x == 0) {
                 st->abs_wl = num;
                 st->abs_dens = den;
@@ -766,13 +874,15 @@ __global__ void __launch_bounds__(kThreads) k_force(
         }
         return;
     }
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < NM; p += gridDim.x * blockDim.x) {
+    for (int p = bid * blockDim.x + threadIdx.x; p < NM; p += nblk * blockDim.x) {
         const int i = perm[p];
         const float2 q = xy[i];
         const float4 o = soff[p];   // offx, offy, cw, ch of cell i
         dgp[p] = force(q.x + o.x, q.y + o.y, o.z, o.w, sratio[p]);
     }
 }
+__global__ void __launch_bounds__(kThreads) k_force(const __grid_constant__ ForceP p) { force_body(p, blockIdx.x, gridDim.x); }
+
 
 // energy = sum psi * rho (src/epotential.rs:344-346), double-float sums
 __global__ void k_energy(size_t mn, const float *__restrict__ psi, const float *__restrict__ rho,
@@ -868,18 +978,49 @@ __device__ __forceinline__ void nesterov_grad_cell(float wlx, float wly, float d
     denf += ddx * ddx + ddy * ddy;
 }
 
-__global__ void __launch_bounds__(kThreads) k_nesterov_grad(
-    int NM, int iter_arg, const float *__restrict__ wlgx, const float *__restrict__ wlgy,
-    const float2 *__restrict__ dgp, const int32_t *__restrict__ pos, const float *__restrict__ w,
-    const float *__restrict__ h, const float *__restrict__ npins, const float *__restrict__ x,
-    const float *__restrict__ y, const float *__restrict__ px, const float *__restrict__ py,
-    float *__restrict__ pgx, float *__restrict__ pgy, double *__restrict__ partials, DevState *st) {
+struct GradP {
+    int NM;
+    int iter_arg;
+    const float * wlgx;
+    const float * wlgy;
+    const float2 * dgp;
+    const int32_t * pos;
+    const float * w;
+    const float * h;
+    const float * npins;
+    const float * x;
+    const float * y;
+    const float * px;
+    const float * py;
+    float * pgx;
+    float * pgy;
+    double * partials;
+    DevState * st;
+};
+__device__ __forceinline__ void nesterov_grad_body(const GradP &p, int bid, int nblk) {
+    int NM = p.NM;
+    int iter_arg = p.iter_arg;
+    const float *__restrict__ wlgx = p.wlgx;
+    const float *__restrict__ wlgy = p.wlgy;
+    const float2 *__restrict__ dgp = p.dgp;
+    const int32_t *__restrict__ pos = p.pos;
+    const float *__restrict__ w = p.w;
+    const float *__restrict__ h = p.h;
+    const float *__restrict__ npins = p.npins;
+    const float *__restrict__ x = p.x;
+    const float *__restrict__ y = p.y;
+    const float *__restrict__ px = p.px;
+    const float *__restrict__ py = p.py;
+    float *__restrict__ pgx = p.pgx;
+    float *__restrict__ pgy = p.pgy;
+    double *__restrict__ partials = p.partials;
+    DevState * st = p.st;
     __shared__ double shr[kThreads / 32];
     if (st->done) return;
     const float dw = st->dw;
     float numf = 0.0f, denf = 0.0f;
     const int n4 = NM >> 2;
-    for (int i4 = blockIdx.x * blockDim.x + threadIdx.x; i4 < n4; i4 += gridDim.x * blockDim.x) {
+    for (int i4 = bid * blockDim.x + threadIdx.x; i4 < n4; i4 += nblk * blockDim.x) {
         const Cell4 a = ld4(wlgx, i4), b = ld4(wlgy, i4);
         const int4 at = reinterpret_cast<const int4 *>(pos)[i4];
         const float2 g0 = dgp[at.x], g1 = dgp[at.y], g2 = dgp[at.z], g3 = dgp[at.w];
@@ -894,7 +1035,7 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_grad(
         st4(pgx, i4, gx);
         st4(pgy, i4, gy);
     }
-    if (blockIdx.x == 0 && threadIdx.x < (NM & 3)) {   // tail cells
+    if (bid == 0 && threadIdx.x < (NM & 3)) {   // tail cells
         const int i = (n4 << 2) + threadIdx.x;
         float gx = pgx[i], gy = pgy[i];
         const float2 g = dgp[pos[i]];
@@ -906,9 +1047,9 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_grad(
     Df vals[2];
     vals[0] = block_sum(numf, shr);
     vals[1] = block_sum(denf, shr);
-    if (arrive_last(partials, blockIdx.x, 2, vals, &st->ctr[CTR_LIP], gridDim.x)) {
-        const double tn = sum_partials(partials, gridDim.x, 2, 0, shr);
-        const double td = sum_partials(partials, gridDim.x, 2, 1, shr);
+    if (arrive_last(partials, bid, 2, vals, &st->ctr[CTR_LIP], nblk)) {
+        const double tn = sum_partials(partials, nblk, 2, 0, shr);
+        const double td = sum_partials(partials, nblk, 2, 1, shr);
         if (threadIdx.x == 0) {
             const int it = iter_arg >= 0 ? iter_arg : st->iteration;
             const float one = 1.0f, two = one + one, four = two + two;
@@ -923,6 +1064,8 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_grad(
         }
     }
 }
+__global__ void __launch_bounds__(kThreads) k_nesterov_grad(const __grid_constant__ GradP p) { nesterov_grad_body(p, blockIdx.x, gridDim.x); }
+
 
 // Lookahead + gradient step + clamp + history (src/nesterov.rs:111-145).
 __device__ __forceinline__ void nesterov_update_cell(float &x, float &y, float &px, float &py, float gx,
@@ -942,15 +1085,39 @@ __device__ __forceinline__ void nesterov_update_cell(float &x, float &y, float &
     y = ny;
 }
 
-__global__ void __launch_bounds__(kThreads) k_nesterov_update(
-    int NM, const float *__restrict__ w, const float *__restrict__ h, float die_w, float die_h,
-    float *__restrict__ x, float *__restrict__ y, float *__restrict__ px, float *__restrict__ py,
-    const float *__restrict__ gx, const float *__restrict__ gy, float2 *__restrict__ xy,
-    const DevState *__restrict__ st) {
+struct UpdateP {
+    int NM;
+    const float * w;
+    const float * h;
+    float die_w;
+    float die_h;
+    float * x;
+    float * y;
+    float * px;
+    float * py;
+    const float * gx;
+    const float * gy;
+    float2 * xy;
+    const DevState * st;
+};
+__device__ __forceinline__ void nesterov_update_body(const UpdateP &p, int bid, int nblk) {
+    int NM = p.NM;
+    const float *__restrict__ w = p.w;
+    const float *__restrict__ h = p.h;
+    float die_w = p.die_w;
+    float die_h = p.die_h;
+    float *__restrict__ x = p.x;
+    float *__restrict__ y = p.y;
+    float *__restrict__ px = p.px;
+    float *__restrict__ py = p.py;
+    const float *__restrict__ gx = p.gx;
+    const float *__restrict__ gy = p.gy;
+    float2 *__restrict__ xy = p.xy;
+    const DevState *__restrict__ st = p.st;
     if (st->done) return;
     const float alpha = st->alpha, beta = st->beta;
     const int n4 = NM >> 2;
-    for (int i4 = blockIdx.x * blockDim.x + threadIdx.x; i4 < n4; i4 += gridDim.x * blockDim.x) {
+    for (int i4 = bid * blockDim.x + threadIdx.x; i4 < n4; i4 += nblk * blockDim.x) {
         Cell4 xx = ld4w(x, i4), yy = ld4w(y, i4), qx = ld4w(px, i4), qy = ld4w(py, i4);
         const Cell4 a = ld4(gx, i4), b = ld4(gy, i4), ww = ld4(w, i4), hh = ld4(h, i4);
 #pragma unroll
@@ -965,7 +1132,7 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_update(
         xy4[0] = make_float4(xx.v[0], yy.v[0], xx.v[1], yy.v[1]);
         xy4[1] = make_float4(xx.v[2], yy.v[2], xx.v[3], yy.v[3]);
     }
-    if (blockIdx.x == 0 && threadIdx.x < (NM & 3)) {
+    if (bid == 0 && threadIdx.x < (NM & 3)) {
         const int i = (n4 << 2) + threadIdx.x;
         float xi = x[i], yi = y[i], pxi = px[i], pyi = py[i];
         nesterov_update_cell(xi, yi, pxi, pyi, gx[i], gy[i], w[i], h[i], die_w, die_h, alpha, beta);
@@ -976,6 +1143,8 @@ __global__ void __launch_bounds__(kThreads) k_nesterov_update(
         xy[i] = make_float2(xi, yi);
     }
 }
+__global__ void __launch_bounds__(kThreads) k_nesterov_update(const __grid_constant__ UpdateP p) { nesterov_update_body(p, blockIdx.x, gridDim.x); }
+
 
 // xy = (x, y) for every instance, after positions were written from the host.
 __global__ void k_pack_xy(int N, const float *__restrict__ x, const float *__restrict__ y,
@@ -1012,8 +1181,20 @@ struct SchedLogs {
 
 // Scheduler::update + should_stop (src/scheduler.rs:68-130) in FP64, plus the
 // step record, the non-finite check and the retire-at-overflow flag.
-__global__ void k_scheduler(int use_args, float hpwl_arg, float ovf_arg, SchedLogs lg, DevState *st) {
-    if (blockIdx.x != 0) return;
+struct SchedP {
+    int use_args;
+    float hpwl_arg;
+    float ovf_arg;
+    SchedLogs lg;
+    DevState * st;
+};
+__device__ __forceinline__ void scheduler_body(const SchedP &p, int bid, int nblk) {
+    int use_args = p.use_args;
+    float hpwl_arg = p.hpwl_arg;
+    float ovf_arg = p.ovf_arg;
+    SchedLogs lg = p.lg;
+    DevState * st = p.st;
+    if (bid != 0) return;
     if (st->done) return;   // warp-uniform
     const float hpwl = use_args ? hpwl_arg : st->hpwl_f;
     const float ovf = use_args ? ovf_arg : st->overflow_f;
@@ -1079,6 +1260,8 @@ __global__ void k_scheduler(int use_args, float hpwl_arg, float ovf_arg, SchedLo
     if (st->stop_overflow > 0.0f && ovf <= st->stop_overflow) st->done = 1;
     if (st->stop_iter > 0 && st->iteration >= st->stop_iter) st->done = 1;
 }
+__global__ void k_scheduler(const __grid_constant__ SchedP p) { scheduler_body(p, blockIdx.x, gridDim.x); }
+
 
 __global__ void k_gather_done(DevState *const *states, int count, int32_t *out) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
@@ -1095,7 +1278,7 @@ static int grid_for(int work, int cap = 152 * 8) {
     return g < 1 ? 1 : (g > cap ? cap : g);
 }
 
-void launch_wirelength(Ctx &c, float gamma_arg) {
+static int wa_params(Ctx &c, float gamma_arg, WaP &p) {
     WaArgs a;
     a.net_ptr = c.net_ptr;
     a.slot_cell = c.slot_cell;
@@ -1133,16 +1316,29 @@ void launch_wirelength(Ctx &c, float gamma_arg) {
         blocks += (int)g;
     }
     cl.block0[kNumClasses] = blocks;
+    p = WaP{a, cl, gamma_arg, c.partials, c.st};
+    return blocks;
+}
+
+void launch_wirelength(Ctx &c, float gamma_arg) {
+    WaP p;
+    const int blocks = wa_params(c, gamma_arg, p);
     if (blocks == 0) {   // no nets: the total is zero
         k_wl_zero<<<1, 32, 0, c.stream>>>(c.st);
         return;
     }
-    k_wa<<<blocks, kThreads, 0, c.stream>>>(a, cl, gamma_arg, c.partials, c.st);
+    k_wa<<<blocks, kThreads, 0, c.stream>>>(p);
+}
+
+static int gather_params(Ctx &c, GatherP &p) {
+    p = GatherP{c.NM, c.cell_slot_ptr, c.cell_slots, c.slot_grad, c.wlgx, c.wlgy, c.st};
+    return grid_for(c.NM);
 }
 
 void launch_wl_gather(Ctx &c) {
-    k_wl_gather<<<grid_for(c.NM), kThreads, 0, c.stream>>>(c.NM, c.cell_slot_ptr, c.cell_slots,
-               c.slot_grad, c.wlgx, c.wlgy, c.st);
+    GatherP p;
+    const int g = gather_params(c, p);
+    k_wl_gather<<<g, kThreads, 0, c.stream>>>(p);
 }
 
 // Blocks of the scatter.  Alone, a context spreads its cells over up to 608
@@ -1150,15 +1346,21 @@ void launch_wl_gather(Ctx &c) {
 // instances on the GPU at once fewer, fuller blocks flush fewer windows (see
 // erp_batch_create).  Never more than kMaxCellsPerBlock cells per block (the
 // window's 21-bit pieces rely on it); the grid decides no bit of the map.
-void launch_density_scatter(Ctx &c) {
+static int scatter_params(Ctx &c, ScatterP &p) {
     const int floor_g = (c.NM + kMaxCellsPerBlock - 1) / kMaxCellsPerBlock;
     const int g = c.scatter_cells > 0 ? std::max((c.NM + c.scatter_cells - 1) / c.scatter_cells, std::max(floor_g, 1))
                                       : std::max(grid_for(c.NM, 152 * 4), floor_g);
     const int nty = (c.n + kSortTile - 1) / kSortTile;
+    p = ScatterP{c.NM, c.perm, c.xy, c.soff, c.sratio, c.skey, nty, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw, c.inv_bh,
+                 c.fixed_scale, c.dmap, c.st};
+    return g;
+}
+
+void launch_density_scatter(Ctx &c) {
+    ScatterP p;
+    const int g = scatter_params(c, p);
     auto kern = c.scatter_planes == 2 ? k_density_scatter<2> : k_density_scatter<3>;
-    kern<<<g, kThreads, density_scatter_smem(c.scatter_planes), c.stream>>>(c.NM, c.perm, c.xy, c.soff,
-               c.sratio, c.skey, nty, c.m, c.n, c.bin_w, c.bin_h, c.inv_bw, c.inv_bh, c.fixed_scale, c.dmap,
-               c.st);
+    kern<<<g, kThreads, density_scatter_smem(c.scatter_planes), c.stream>>>(p);
 }
 
 void launch_scatter_order(Ctx &c, cudaStream_t s) {
@@ -1217,10 +1419,16 @@ static int fit(int need, const std::atomic<int> &resident_a) {
     return resident > 0 && need > resident ? resident : need;
 }
 
+static int force_params(Ctx &c, int rescale, ForceP &p) {
+    p = ForceP{c.NM, c.perm, c.xy, c.soff, c.sratio, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w,
+               c.bin_h, c.inv_bw, c.inv_bh, c.fx, c.fy, c.dgp, c.pos, rescale, c.wlgx, c.wlgy, c.partials, c.st};
+    return fit(grid_for(c.NM, 152 * 16), g_res_force);
+}
+
 void launch_force(Ctx &c, int rescale) {
-    k_force<<<fit(grid_for(c.NM, 152 * 16), g_res_force), kThreads, 0, c.stream>>>(
-               c.NM, c.perm, c.xy, c.soff, c.sratio, c.offx, c.offy, c.cw, c.ch, c.ratio, c.m, c.n, c.bin_w,
-               c.bin_h, c.inv_bw, c.inv_bh, c.fx, c.fy, c.dgp, c.pos, rescale, c.wlgx, c.wlgy, c.partials, c.st);
+    ForceP p;
+    const int g = force_params(c, rescale, p);
+    k_force<<<g, kThreads, 0, c.stream>>>(p);
 }
 
 void launch_energy(Ctx &c) {
@@ -1229,17 +1437,28 @@ void launch_energy(Ctx &c) {
         mn, c.psi, c.rho, c.partials, c.st);
 }
 
+static int grad_params(Ctx &c, int iter_arg, GradP &p) {
+    p = GradP{c.NM, iter_arg, c.wlgx, c.wlgy, c.dgp, c.pos, c.w, c.h, c.npins, c.x, c.y, c.prev_x, c.prev_y,
+              c.prev_gx, c.prev_gy, c.partials, c.st};
+    return fit(grid_for((c.NM + 3) / 4), g_res_grad);
+}
+
+static int update_params(Ctx &c, UpdateP &p) {
+    p = UpdateP{c.NM, c.w, c.h, c.die_w, c.die_h, c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.xy, c.st};
+    return fit(grid_for((c.NM + 3) / 4), g_res_update);
+}
+
 void launch_nesterov(Ctx &c, int iter_arg) {
     if (iter_arg >= 0) {   // stage entry point; in the step graph k_force does the rescale
         const int g = grid_for(c.NM);
         k_dw_rescale<<<g, kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgp, c.pos,
                                                    c.partials, c.st);
     }
-    const int g4 = grid_for((c.NM + 3) / 4);
-    k_nesterov_grad<<<fit(g4, g_res_grad), kThreads, 0, c.stream>>>(c.NM, iter_arg, c.wlgx, c.wlgy, c.dgp,
-               c.pos, c.w, c.h, c.npins, c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.partials, c.st);
-    k_nesterov_update<<<fit(g4, g_res_update), kThreads, 0, c.stream>>>(c.NM, c.w, c.h, c.die_w, c.die_h,
-               c.x, c.y, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.xy, c.st);
+    GradP pg;
+    UpdateP pu;
+    const int gg = grad_params(c, iter_arg, pg), gu = update_params(c, pu);
+    k_nesterov_grad<<<gg, kThreads, 0, c.stream>>>(pg);
+    k_nesterov_update<<<gu, kThreads, 0, c.stream>>>(pu);
 }
 
 cudaError_t place_occupancy() {
@@ -1315,11 +1534,120 @@ void launch_xy_to_host(Ctx &c, float *hx, float *hy) {
     k_xy_to_host<<<grid_for(c.N), kThreads, 0, c.stream>>>(c.N, c.xy, hx, hy);
 }
 
-void launch_scheduler(Ctx &c, int use_args, float hpwl, float overflow) {
-    // update_density_weight's bases 0.9999 and 1.05, update_gamma's 10
-    // (src/scheduler.rs:92-130)
+// update_density_weight's bases 0.9999 and 1.05, update_gamma's 10
+// (src/scheduler.rs:92-130)
+static SchedP sched_params(Ctx &c, int use_args, float hpwl, float overflow) {
     static const SchedLogs lg = {std::log(0.9999), std::log(1.05), std::log(10.0)};
-    k_scheduler<<<1, 32, 0, c.stream>>>(use_args, hpwl, overflow, lg, c.st);
+    return SchedP{use_args, hpwl, overflow, lg, c.st};
+}
+
+void launch_scheduler(Ctx &c, int use_args, float hpwl, float overflow) {
+    k_scheduler<<<1, 32, 0, c.stream>>>(sched_params(c, use_args, hpwl, overflow));
+}
+
+// ---- packed launches (batches) ----
+template <typename P, typename F>
+static void plan_stage(PackKind k, int variant, const std::vector<Ctx *> &xs, PackedArena &ar,
+                       std::vector<PackedLaunch> &out, int threads, size_t smem, F params) {
+    std::vector<P> tab;
+    std::vector<int32_t> block0(1, 0);
+    for (Ctx *c : xs) {
+        P p;
+        const int g = params(*c, p);
+        if (g <= 0) continue;
+        tab.push_back(p);
+        block0.push_back(block0.back() + g);
+    }
+    if (tab.empty()) return;
+    PackedLaunch l;
+    l.kind = k;
+    l.variant = variant;
+    l.tab = ar.put(tab.data(), sizeof(P) * tab.size());
+    l.block0 = ar.put(block0.data(), sizeof(int32_t) * block0.size());
+    l.n = (int)tab.size();
+    l.blocks = block0.back();
+    l.threads = threads;
+    l.smem = smem;
+    out.push_back(l);
+}
+
+void packed_place_stage(PackKind k, const std::vector<Ctx *> &xs, PackedArena &ar, std::vector<PackedLaunch> &out) {
+    switch (k) {
+    case PK_WA:
+        plan_stage<WaP>(k, 0, xs, ar, out, kThreads, 0, [](Ctx &c, WaP &p) { return wa_params(c, -1.0f, p); });
+        break;
+    case PK_GATHER:
+        plan_stage<GatherP>(k, 0, xs, ar, out, kThreads, 0, [](Ctx &c, GatherP &p) { return gather_params(c, p); });
+        break;
+    case PK_SCATTER:
+        for (int planes = 2; planes <= 3; ++planes) {
+            std::vector<Ctx *> sub;
+            for (Ctx *c : xs)
+                if (c->scatter_planes == planes) sub.push_back(c);
+            plan_stage<ScatterP>(k, planes, sub, ar, out, kThreads, density_scatter_smem(planes),
+                                 [](Ctx &c, ScatterP &p) { return scatter_params(c, p); });
+        }
+        break;
+    case PK_FORCE:
+        plan_stage<ForceP>(k, 0, xs, ar, out, kThreads, 0, [](Ctx &c, ForceP &p) { return force_params(c, 1, p); });
+        break;
+    case PK_GRAD:
+        plan_stage<GradP>(k, 0, xs, ar, out, kThreads, 0, [](Ctx &c, GradP &p) { return grad_params(c, -1, p); });
+        break;
+    case PK_UPDATE:
+        plan_stage<UpdateP>(k, 0, xs, ar, out, kThreads, 0, [](Ctx &c, UpdateP &p) { return update_params(c, p); });
+        break;
+    case PK_SCHED:
+        plan_stage<SchedP>(k, 0, xs, ar, out, 32, 0, [](Ctx &c, SchedP &p) {
+            p = sched_params(c, 0, 0.f, 0.f);
+            return 1;
+        });
+        break;
+    default:
+        break;
+    }
+}
+
+static cudaError_t packed_prepare() {
+    cudaError_t e = cudaFuncSetAttribute(k_packed<ScatterP, density_scatter_body<2>, kThreads, 4>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)density_scatter_smem(2));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_packed<ScatterP, density_scatter_body<3>, kThreads, 4>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)density_scatter_smem(3));
+}
+
+bool packed_place_launch(const PackedLaunch &l, const unsigned char *dev, cudaStream_t s) {
+    switch (l.kind) {
+    case PK_WA:
+        k_packed<WaP, wa_body, kThreads, 4><<<l.blocks, l.threads, 0, s>>>(packed_args<WaP>(l, dev));
+        return true;
+    case PK_GATHER:
+        k_packed<GatherP, wl_gather_body, kThreads, 4><<<l.blocks, l.threads, 0, s>>>(packed_args<GatherP>(l, dev));
+        return true;
+    case PK_SCATTER:
+        if (l.variant == 2)
+            k_packed<ScatterP, density_scatter_body<2>, kThreads, 4><<<l.blocks, l.threads, l.smem, s>>>(
+                packed_args<ScatterP>(l, dev));
+        else
+            k_packed<ScatterP, density_scatter_body<3>, kThreads, 4><<<l.blocks, l.threads, l.smem, s>>>(
+                packed_args<ScatterP>(l, dev));
+        return true;
+    case PK_FORCE:
+        k_packed<ForceP, force_body, kThreads, 4><<<l.blocks, l.threads, 0, s>>>(packed_args<ForceP>(l, dev));
+        return true;
+    case PK_GRAD:
+        k_packed<GradP, nesterov_grad_body, kThreads, 3><<<l.blocks, l.threads, 0, s>>>(packed_args<GradP>(l, dev));
+        return true;
+    case PK_UPDATE:
+        k_packed<UpdateP, nesterov_update_body, kThreads, 4><<<l.blocks, l.threads, 0, s>>>(
+            packed_args<UpdateP>(l, dev));
+        return true;
+    case PK_SCHED:
+        k_packed<SchedP, scheduler_body, 32, 1><<<l.blocks, l.threads, 0, s>>>(packed_args<SchedP>(l, dev));
+        return true;
+    default:
+        return false;
+    }
 }
 
 }  // namespace erp

@@ -478,20 +478,47 @@ __device__ __forceinline__ void warp_inv_real(XFn x, bool sine, float2 *zb, cons
 // on the warp's mbarrier, so the whole row arrives at copy bandwidth while the
 // block loads the axis tables; the lanes then convert from shared memory and
 // zero the row with 16-byte stores.
+struct RowsDctWP {
+    int m;
+    const float2 * tw_n;
+    const float2 * ek_n;
+    const float * rho_in;
+    unsigned long long * dmap;
+    const float * initial;
+    float fixed_inv;
+    float coef;
+    float inv_area;
+    int zero_map;
+    float * rho_out;
+    float * t1;
+    double * partials;
+    DevState * st;
+    double movable_area;
+};
 template <int E, int NW>
-__global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
-    int m, const float2 *__restrict__ tw_n, const float2 *__restrict__ ek_n,
-    const float *__restrict__ rho_in, unsigned long long *__restrict__ dmap,
-    const float *__restrict__ initial, float fixed_inv, float coef, float inv_area, int zero_map,
-    float *__restrict__ rho_out, float *__restrict__ t1, double *__restrict__ partials,
-    DevState *__restrict__ st, double movable_area) {
+__device__ __forceinline__ void rows_dct_w_body(const RowsDctWP &p, int bid, int nblk) {
+    int m = p.m;
+    const float2 *__restrict__ tw_n = p.tw_n;
+    const float2 *__restrict__ ek_n = p.ek_n;
+    const float *__restrict__ rho_in = p.rho_in;
+    unsigned long long *__restrict__ dmap = p.dmap;
+    const float *__restrict__ initial = p.initial;
+    float fixed_inv = p.fixed_inv;
+    float coef = p.coef;
+    float inv_area = p.inv_area;
+    int zero_map = p.zero_map;
+    float *__restrict__ rho_out = p.rho_out;
+    float *__restrict__ t1 = p.t1;
+    double *__restrict__ partials = p.partials;
+    DevState *__restrict__ st = p.st;
+    double movable_area = p.movable_area;
     constexpr int H = 32 * E, N = 2 * H;
     if (st && st->done) return;
     extern __shared__ __align__(16) float2 sm[];
     __shared__ __align__(8) uint64_t bar[NW];
     __shared__ double shr[NW];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = blockIdx.x * NW + warp;
+    const int row = bid * NW + warp;
     float2 *wbase = sm + tables_f2<H>() + warp * 3 * H;   // [2H float2 work | N float stage]
     float *xm = reinterpret_cast<float *>(wbase);
     float2 *zb = wbase + H;
@@ -551,8 +578,8 @@ __global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
     warp_dct2_real<E>(xm, zb, tb.twh, tb.tw, tb.ek, lane, [&](int k, float y) { out[k] = y; });
     if (from_map && partials) {
         const Df vals[1] = {block_sum(ovf, shr)};
-        if (arrive_last(partials, blockIdx.x, 1, vals, &st->ctr[CTR_OVF], gridDim.x)) {
-            const double tot = sum_partials(partials, gridDim.x, 1, 0, shr);
+        if (arrive_last(partials, bid, 1, vals, &st->ctr[CTR_OVF], nblk)) {
+            const double tot = sum_partials(partials, nblk, 1, 0, shr);
             if (threadIdx.x == 0) {
                 st->overflow = tot;
                 st->overflow_f = (float)(tot / movable_area);
@@ -561,17 +588,40 @@ __global__ void __launch_bounds__(NW * 32) k_rows_dct_w(
         }
     }
 }
+template <int E, int NW>
+__global__ void __launch_bounds__(NW * 32) k_rows_dct_w(const __grid_constant__ RowsDctWP p) { rows_dct_w_body<E, NW>(p, blockIdx.x, gridDim.x); }
+
 
 // C1 (warp form): NW columns per block, one warp per column.  Coalesced tile
 // load, forward DCT-II along x, A and the column's 1/(wu^2+wv^2) kept in shared
 // memory (one division per bin), then for each output kind the weighted inverse
 // along x and a coalesced tile store.
+struct ColsWP {
+    int n;
+    const float2 * tw_m;
+    const float2 * ek_m;
+    const float * wu_g;
+    const float * wv;
+    const float * t1;
+    float * tx;
+    float * ty;
+    float * tp;
+    float scale4;
+    const DevState * st;
+};
 template <int E, int NW>
-__global__ void __launch_bounds__(NW * 32) k_cols_w(
-    int n, const float2 *__restrict__ tw_m, const float2 *__restrict__ ek_m,
-    const float *__restrict__ wu_g, const float *__restrict__ wv, const float *__restrict__ t1,
-    float *__restrict__ tx, float *__restrict__ ty, float *__restrict__ tp, float scale4,
-    const DevState *__restrict__ st) {
+__device__ __forceinline__ void cols_w_body(const ColsWP &p, int bid, int nblk) {
+    int n = p.n;
+    const float2 *__restrict__ tw_m = p.tw_m;
+    const float2 *__restrict__ ek_m = p.ek_m;
+    const float *__restrict__ wu_g = p.wu_g;
+    const float *__restrict__ wv = p.wv;
+    const float *__restrict__ t1 = p.t1;
+    float *__restrict__ tx = p.tx;
+    float *__restrict__ ty = p.ty;
+    float *__restrict__ tp = p.tp;
+    float scale4 = p.scale4;
+    const DevState *__restrict__ st = p.st;
     constexpr int H = 32 * E, M = 2 * H;
     constexpr int S = NW + 1;   // tile row stride (odd: conflict-free row-wise access)
     if (st && st->done) return;
@@ -584,7 +634,7 @@ __global__ void __launch_bounds__(NW * 32) k_cols_w(
     float2 *zb = reinterpret_cast<float2 *>(ib + M);                             // FFT staging
     float *wu = reinterpret_cast<float *>(sm + tables_f2<H>() + NW * 3 * H);
     float *tile = wu + M;
-    const int j0 = blockIdx.x * NW;
+    const int j0 = bid * NW;
     for (int k = threadIdx.x; k < M; k += NW * 32) wu[k] = wu_g[k];
     for (int idx = threadIdx.x; idx < M * NW; idx += NW * 32) {
         const int i = idx / NW, c = idx - i * NW;
@@ -650,14 +700,37 @@ __global__ void __launch_bounds__(NW * 32) k_cols_w(
         __syncthreads();
     }
 }
+template <int E, int NW>
+__global__ void __launch_bounds__(NW * 32) k_cols_w(const __grid_constant__ ColsWP p) { cols_w_body<E, NW>(p, blockIdx.x, gridDim.x); }
+
 
 // R2 (warp form): rows inverse along y, one warp per (row, output kind).
+struct RowsInvWP {
+    int m;
+    int nkinds;
+    const float2 * tw_n;
+    const float2 * ek_n;
+    const float * tx;
+    const float * ty;
+    const float * tp;
+    float * fx;
+    float * fy;
+    float * psi;
+    const DevState * st;
+};
 template <int E, int NW>
-__global__ void __launch_bounds__(NW * 32) k_rows_inv_w(
-    int m, int nkinds, const float2 *__restrict__ tw_n, const float2 *__restrict__ ek_n,
-    const float *__restrict__ tx, const float *__restrict__ ty, const float *__restrict__ tp,
-    float *__restrict__ fx, float *__restrict__ fy, float *__restrict__ psi,
-    const DevState *__restrict__ st) {
+__device__ __forceinline__ void rows_inv_w_body(const RowsInvWP &p, int bid, int nblk) {
+    int m = p.m;
+    int nkinds = p.nkinds;
+    const float2 *__restrict__ tw_n = p.tw_n;
+    const float2 *__restrict__ ek_n = p.ek_n;
+    const float *__restrict__ tx = p.tx;
+    const float *__restrict__ ty = p.ty;
+    const float *__restrict__ tp = p.tp;
+    float *__restrict__ fx = p.fx;
+    float *__restrict__ fy = p.fy;
+    float *__restrict__ psi = p.psi;
+    const DevState *__restrict__ st = p.st;
     constexpr int H = 32 * E, N = 2 * H;
     if (st && st->done) return;
     extern __shared__ __align__(16) float2 sm[];
@@ -666,7 +739,7 @@ __global__ void __launch_bounds__(NW * 32) k_rows_inv_w(
     float *xb = reinterpret_cast<float *>(sm + tables_f2<H>() + warp * 2 * H);
     float2 *zb = sm + tables_f2<H>() + warp * 2 * H + H;
     __syncthreads();
-    const int task = blockIdx.x * NW + warp;
+    const int task = bid * NW + warp;
     const int row = task / nkinds, kind = task - row * nkinds;
     // kind 0: field_x = IDCT_y(tx); kind 1: field_y = IDXST_y(ty); kind 2: psi = IDCT_y(tp)
     const float *in = (kind == 0 ? tx : (kind == 1 ? ty : tp)) + (size_t)row * N;
@@ -677,6 +750,9 @@ __global__ void __launch_bounds__(NW * 32) k_rows_inv_w(
     warp_inv_real<E>([&](int u) { return xb[u]; }, kind == 1, zb, tb.twh, tb.tw, tb.ek, lane,
                      [&](int i, float v) { out[i] = v; });
 }
+template <int E, int NW>
+__global__ void __launch_bounds__(NW * 32) k_rows_inv_w(const __grid_constant__ RowsInvWP p) { rows_inv_w_body<E, NW>(p, blockIdx.x, gridDim.x); }
+
 
 // ===================================================================
 // Group transforms: kQ = 4 warps per sequence (sides 512..2048).  At a 1024^2
@@ -1196,20 +1272,20 @@ static bool warp_side(int v) { return v >= 64 && v <= 2048; }
 
 template <int E, int NW>
 static void rows_dct_w_nw(const SpectralPlan &p, const SpectralArgs &a, bool from_map) {
-    k_rows_dct_w<E, NW><<<p.m / NW, NW * 32, rows_dct_w_smem<E, NW>(), p.stream>>>(
+    k_rows_dct_w<E, NW><<<p.m / NW, NW * 32, rows_dct_w_smem<E, NW>(), p.stream>>>(RowsDctWP{
         p.m, p.tw_n, p.ek_n, a.rho_in, a.dmap, a.initial, a.fixed_inv, a.coef, a.inv_bin_area,
-        a.zero_map ? 1 : 0, a.rho_out, p.t1, from_map ? a.partials : nullptr, a.st, a.movable_area);
+        a.zero_map ? 1 : 0, a.rho_out, p.t1, from_map ? a.partials : nullptr, a.st, a.movable_area});
 }
 template <int E, int NW>
 static void cols_w_nw(const SpectralPlan &p, const SpectralArgs &a, float scale4, float *tp) {
-    k_cols_w<E, NW><<<p.n / NW, NW * 32, cols_w_smem<E, NW>(), p.stream>>>(
-        p.n, p.tw_m, p.ek_m, p.wu, p.wv, p.t1, p.tx, p.ty, tp, scale4, a.st);
+    k_cols_w<E, NW><<<p.n / NW, NW * 32, cols_w_smem<E, NW>(), p.stream>>>(ColsWP{
+        p.n, p.tw_m, p.ek_m, p.wu, p.wv, p.t1, p.tx, p.ty, tp, scale4, a.st});
 }
 template <int E, int NW>
 static void rows_inv_w_nw(const SpectralPlan &p, const SpectralArgs &a, float *tp) {
     const int nk = tp ? 3 : 2;
-    k_rows_inv_w<E, NW><<<p.m * nk / NW, NW * 32, rows_w_smem<E, NW>(), p.stream>>>(
-        p.m, nk, p.tw_n, p.ek_n, p.tx, p.ty, tp, a.fx, a.fy, a.psi, a.st);
+    k_rows_inv_w<E, NW><<<p.m * nk / NW, NW * 32, rows_w_smem<E, NW>(), p.stream>>>(RowsInvWP{
+        p.m, nk, p.tw_n, p.ek_n, p.tx, p.ty, tp, a.fx, a.fy, a.psi, a.st});
 }
 // the plan's sequences per block: an autotuned alternative (sides 64..256) or
 // the fixed shape
@@ -1285,6 +1361,134 @@ void launch_spectral_plan(const SpectralPlan &p, const SpectralArgs &a) {
         k_rows_inv<kRowPairs><<<rb, kThreads, rows_smem(n, kRowPairs), p.stream>>>(
             m, n, p.logn, p.tw_n, p.ek_n, p.tx, p.ty, tp, a.fx, a.fy, a.psi, a.st);
     }
+}
+
+// ---- packed launches of the warp-form passes (batches) ----
+// Sides 64..256: each pass of many solves in one launch per (E, NW) in use.
+static int packed_nw(const SpectralPlan &p, int E, int fixed) {
+    return (E <= 4 && (p.seqs == kSeqCandidates[0] || p.seqs == kSeqCandidates[1])) ? p.seqs : fixed;
+}
+
+template <typename P>
+static void plan_spectral(PackKind k, int variant, const std::vector<const SpectralJob *> &js, PackedArena &ar,
+                          std::vector<PackedLaunch> &out, size_t smem, int threads,
+                          P (*params)(const SpectralJob &, int &grid)) {
+    std::vector<P> tab;
+    std::vector<int32_t> block0(1, 0);
+    for (const SpectralJob *j : js) {
+        int g = 0;
+        tab.push_back(params(*j, g));
+        block0.push_back(block0.back() + g);
+    }
+    if (tab.empty()) return;
+    PackedLaunch l;
+    l.kind = k;
+    l.variant = variant;
+    l.tab = ar.put(tab.data(), sizeof(P) * tab.size());
+    l.block0 = ar.put(block0.data(), sizeof(int32_t) * block0.size());
+    l.n = (int)tab.size();
+    l.blocks = block0.back();
+    l.threads = threads;
+    l.smem = smem;
+    out.push_back(l);
+}
+
+template <int E, int NW>
+static RowsDctWP rows_dct_w_params(const SpectralJob &j, int &grid) {
+    const SpectralPlan &p = j.p;
+    const SpectralArgs &a = j.a;
+    grid = p.m / NW;
+    return RowsDctWP{p.m, p.tw_n, p.ek_n, a.rho_in, a.dmap, a.initial, a.fixed_inv, a.coef, a.inv_bin_area,
+                     a.zero_map ? 1 : 0, a.rho_out, p.t1, a.rho_in == nullptr ? a.partials : nullptr, a.st,
+                     a.movable_area};
+}
+template <int E, int NW>
+static ColsWP cols_w_params(const SpectralJob &j, int &grid) {
+    const SpectralPlan &p = j.p;
+    const SpectralArgs &a = j.a;
+    grid = p.n / NW;
+    return ColsWP{p.n, p.tw_m, p.ek_m, p.wu, p.wv, p.t1, p.tx, p.ty, a.psi ? p.tp : nullptr,
+                  4.0f / (float)((double)p.m * (double)p.n), a.st};
+}
+template <int E, int NW>
+static RowsInvWP rows_inv_w_params(const SpectralJob &j, int &grid) {
+    const SpectralPlan &p = j.p;
+    const SpectralArgs &a = j.a;
+    const int nk = a.psi ? 3 : 2;
+    grid = p.m * nk / NW;
+    return RowsInvWP{p.m, nk, p.tw_n, p.ek_n, p.tx, p.ty, a.psi ? p.tp : nullptr, a.fx, a.fy, a.psi, a.st};
+}
+
+template <int E, int NW>
+static void plan_spectral_en(PackKind k, const std::vector<const SpectralJob *> &js, PackedArena &ar,
+                             std::vector<PackedLaunch> &out) {
+    const int variant = E * 16 + NW;
+    if (k == PK_ROWS_DCT_W)
+        plan_spectral<RowsDctWP>(k, variant, js, ar, out, rows_dct_w_smem<E, NW>(), NW * 32, rows_dct_w_params<E, NW>);
+    else if (k == PK_COLS_W)
+        plan_spectral<ColsWP>(k, variant, js, ar, out, cols_w_smem<E, NW>(), NW * 32, cols_w_params<E, NW>);
+    else
+        plan_spectral<RowsInvWP>(k, variant, js, ar, out, rows_w_smem<E, NW>(), NW * 32, rows_inv_w_params<E, NW>);
+}
+
+template <int E>
+static void plan_spectral_e(PackKind k, int NW, const std::vector<const SpectralJob *> &js, PackedArena &ar,
+                            std::vector<PackedLaunch> &out) {
+    switch (NW) {
+    case kSeqCandidates[0]: plan_spectral_en<E, kSeqCandidates[0]>(k, js, ar, out); break;
+    case kSeqCandidates[1]: plan_spectral_en<E, kSeqCandidates[1]>(k, js, ar, out); break;
+    default: plan_spectral_en<E, kRowWarps>(k, js, ar, out); break;
+    }
+}
+
+void packed_spectral_stage(PackKind k, const std::vector<SpectralJob> &v, PackedArena &ar,
+                           std::vector<PackedLaunch> &out) {
+    static_assert(kRowWarps == kColWarps, "one fixed shape for rows and columns");
+    for (int E : {1, 2, 4}) {
+        for (int NW : {kSeqCandidates[0], kRowWarps, kSeqCandidates[1]}) {
+            std::vector<const SpectralJob *> js;
+            for (const SpectralJob &j : v) {
+                const int side = k == PK_COLS_W ? j.p.m : j.p.n;
+                if (side != 64 * E) continue;
+                if (packed_nw(j.p, E, kRowWarps) != NW) continue;
+                js.push_back(&j);
+            }
+            if (js.empty()) continue;
+            if (E == 1) plan_spectral_e<1>(k, NW, js, ar, out);
+            else if (E == 2) plan_spectral_e<2>(k, NW, js, ar, out);
+            else plan_spectral_e<4>(k, NW, js, ar, out);
+        }
+    }
+}
+
+template <int E, int NW>
+static void packed_spectral_launch_en(const PackedLaunch &l, const unsigned char *dev, cudaStream_t s) {
+    if (l.kind == PK_ROWS_DCT_W)
+        k_packed<RowsDctWP, rows_dct_w_body<E, NW>, NW * 32, 1><<<l.blocks, NW * 32, l.smem, s>>>(
+            packed_args<RowsDctWP>(l, dev));
+    else if (l.kind == PK_COLS_W)
+        k_packed<ColsWP, cols_w_body<E, NW>, NW * 32, 1><<<l.blocks, NW * 32, l.smem, s>>>(packed_args<ColsWP>(l, dev));
+    else
+        k_packed<RowsInvWP, rows_inv_w_body<E, NW>, NW * 32, 1><<<l.blocks, NW * 32, l.smem, s>>>(
+            packed_args<RowsInvWP>(l, dev));
+}
+
+template <int E>
+static void packed_spectral_launch_e(const PackedLaunch &l, int NW, const unsigned char *dev, cudaStream_t s) {
+    switch (NW) {
+    case kSeqCandidates[0]: packed_spectral_launch_en<E, kSeqCandidates[0]>(l, dev, s); break;
+    case kSeqCandidates[1]: packed_spectral_launch_en<E, kSeqCandidates[1]>(l, dev, s); break;
+    default: packed_spectral_launch_en<E, kRowWarps>(l, dev, s); break;
+    }
+}
+
+bool packed_spectral_launch(const PackedLaunch &l, const unsigned char *dev, cudaStream_t s) {
+    if (l.kind != PK_ROWS_DCT_W && l.kind != PK_COLS_W && l.kind != PK_ROWS_INV_W) return false;
+    const int E = l.variant / 16, NW = l.variant % 16;
+    if (E == 1) packed_spectral_launch_e<1>(l, NW, dev, s);
+    else if (E == 2) packed_spectral_launch_e<2>(l, NW, dev, s);
+    else packed_spectral_launch_e<4>(l, NW, dev, s);
+    return true;
 }
 
 }  // namespace erp

@@ -159,6 +159,7 @@ EXPORTS = {
     "erp_batch_destroy": (None, [C.c_void_p]),
     "erp_batch_tuning": (C.c_int, [C.c_void_p, i32p, i32p, f32p, C.c_int32, i32p]),
     "erp_batch_spectral_tuning": (C.c_int, [C.c_void_p, i32p, i32p, f32p, C.c_int32, i32p]),
+    "erp_batch_packed": (C.c_int, [C.c_void_p, i32p]),
     "erp_synth_create": (C.c_int, [C.POINTER(SynthParams), C.POINTER(C.c_void_p)]),
     "erp_synth_design": (C.c_int, [C.c_void_p, C.POINTER(Design)]),
     "erp_synth_destroy": (None, [C.c_void_p]),

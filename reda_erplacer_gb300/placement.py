@@ -242,6 +242,12 @@ class Batch:
         L.check(self.lib.erp_batch_tuning(self.h, C.byref(ch), cells, ms, 8, C.byref(n)))
         return int(ch.value), [(int(cells[i]), float(ms[i])) for i in range(min(n.value, 8))]
 
+    def packed_instances(self):
+        """How many instances advance in packed launches (erp_batch_packed)."""
+        n = C.c_int32()
+        L.check(self.lib.erp_batch_packed(self.h, C.byref(n)))
+        return int(n.value)
+
     def spectral_tuning(self):
         """The autotuned tile shape of the FP32 spectral passes: (chosen sequences
         per block, 0 for the fixed shape, [(candidate, ms), ...])."""

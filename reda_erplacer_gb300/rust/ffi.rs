@@ -232,6 +232,7 @@ extern "C" {
                             count: *mut i32) -> erp_status;
     pub fn erp_batch_spectral_tuning(b: *const erp_batch, chosen: *mut i32, seqs: *mut i32, ms: *mut f32, cap: i32,
                                      count: *mut i32) -> erp_status;
+    pub fn erp_batch_packed(b: *const erp_batch, packed_instances: *mut i32) -> erp_status;
     pub fn erp_batch_destroy(b: *mut erp_batch);
 
     // a stream of jobs: continuous batching under an HBM budget

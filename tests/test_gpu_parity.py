@@ -431,6 +431,33 @@ def test_batch_spectral_autotune(R):
             del os.environ["ERP_BATCH_SPECTRAL_SEQS"]
 
 
+def test_batch_packed_and_branch_forms_match(R):
+    """The packed launches (small FP32 instances: one launch per stage over a
+    table of all of them) and a graph branch per instance give the same bits;
+    both equal the designs run alone (test_batch_matches_individual_runs runs
+    the default form, the packed one)."""
+    import os
+    mix = R.workload_batch(count=8, seed=79, min_cells=2000, max_cells=60000)
+    designs, bins = [d for d, _ in mix], [b for _, b in mix]
+    res = {}
+    for form in ("packed", "branches"):
+        os.environ["ERP_BATCH_FORM"] = form
+        try:
+            bt = R.Batch(designs, bins, 1.0, start_mode=1)
+        finally:
+            del os.environ["ERP_BATCH_FORM"]
+        packed = bt.packed_instances()
+        its, lasts = bt.run(120, stop_overflow=0.6)
+        res[form] = (packed, its, [(l["hpwl"], l["overflow"]) for l in lasts],
+                     [bt.positions(i) for i in range(len(mix))])
+        bt.close()
+    small = sum(1 for b in bins if max(b) <= 256)
+    assert res["packed"][0] == small > 0 and res["branches"][0] == 0
+    assert res["packed"][1] == res["branches"][1] and res["packed"][2] == res["branches"][2]
+    for (xa, ya), (xb, yb) in zip(res["packed"][3], res["branches"][3]):
+        assert np.array_equal(xa, xb) and np.array_equal(ya, yb)
+
+
 def test_batch_matches_individual_runs(R):
     """Instances advanced together in one batched graph end bit-identical to the
     same designs run alone (each instance's kernels are the same; only their
