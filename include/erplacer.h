@@ -287,8 +287,9 @@ erp_status erp_batch_tuning(const erp_batch *b, int32_t *chosen, int32_t *cells,
 erp_status erp_batch_spectral_tuning(const erp_batch *b, int32_t *chosen, int32_t *seqs, float *ms, int32_t cap,
                                      int32_t *count);
 /* How many of the batch's instances advance in packed launches (no counterpart
- * in the reference): every FP32 instance whose bin grid is 64..256 on both axes
- * (and that has movable cells and nets) runs each stage of its step inside one
+ * in the reference): every FP32 instance whose bin grid is 64..256 on both axes,
+ * with movable cells and nets and at most 100,000 movable cells (the environment
+ * variable ERP_BATCH_PACK_MAX_CELLS sets that cap), runs each stage of its step inside one
  * launch per stage and kernel variant that covers all such instances -- each
  * block finds its instance in a packed table of their arguments -- instead of a
  * graph branch of its own kernels; the rest keep a branch each.  The results are

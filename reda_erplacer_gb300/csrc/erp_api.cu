@@ -1484,10 +1484,20 @@ extern "C" erp_status erp_batch_spectral_tuning(const erp_batch *b, int32_t *cho
 
 // Whether an instance's step runs in the batch's packed launches: the FP32
 // solve in its warp forms (bins 64..256 on both axes), with movable cells and
-// nets.  Larger grids, whose kernels are long enough for their launches not to
-// matter, and the tensor-core solve keep a graph branch each.
+// nets, and at most 100,000 movable cells (ERP_BATCH_PACK_MAX_CELLS sets the
+// cap).  Larger grids, whose kernels are long enough for their launches not to
+// matter, and the tensor-core solve keep a graph branch each; so do the larger
+// instances, which then run beside the packed chain instead of holding up each
+// of its stages (whole runs of the 64-design mix: no cap 501k jobs/h, caps of
+// 100k / 50k / 25k / 12k cells 570k / 567k / 556k / 531k, a branch for every
+// instance 507k).
 static bool packable(const Ctx &c) {
-    return !c.gemm && c.m >= 64 && c.m <= 256 && c.n >= 64 && c.n <= 256 && c.NM > 0 && c.E > 0;
+    static const long long max_cells = [] {
+        const char *v = getenv("ERP_BATCH_PACK_MAX_CELLS");
+        return v ? atoll(v) : 100000LL;
+    }();
+    return !c.gemm && c.m >= 64 && c.m <= 256 && c.n >= 64 && c.n <= 256 && c.NM > 0 && c.E > 0 &&
+           (long long)c.NM <= max_cells;
 }
 
 // The packed launches of one step over xs, in stage order, with their argument

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "erplacer.h"
+#include "packed.h"
 
 namespace erp {
 
@@ -169,26 +170,6 @@ void enqueue_step_kernels(Ctx &c);
 void launch_gather_done(DevState *const *states, int count, int32_t *out, cudaStream_t s);
 
 // ---- packed launches (batches) ----
-// One grid over the blocks of many instances of one kernel: instance i owns
-// blocks [block0[i], block0[i + 1]) and reads its arguments from tab[i].  Each
-// instance's blocks see the block index and the grid size they would have in a
-// launch of their own, so every instance computes the same bits as alone.
-template <typename P>
-struct Packed {
-    const P *tab;
-    const int32_t *block0;
-    int32_t n;
-};
-// the instance that owns block b (block0 ascending, block0[0] = 0)
-__device__ __forceinline__ int packed_instance(const int32_t *__restrict__ block0, int n, int b) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(block0 + mid) <= b) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
 // The packed form of a kernel whose body is BODY(args, block, grid).
 template <typename P, void (*BODY)(const P &, int, int), int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_packed(const __grid_constant__ Packed<P> pk) {

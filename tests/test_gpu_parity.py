@@ -451,7 +451,7 @@ def test_batch_packed_and_branch_forms_match(R):
         res[form] = (packed, its, [(l["hpwl"], l["overflow"]) for l in lasts],
                      [bt.positions(i) for i in range(len(mix))])
         bt.close()
-    small = sum(1 for b in bins if max(b) <= 256)
+    small = sum(1 for d, b in mix if max(b) <= 256 and d.num_movable <= 100000)
     assert res["packed"][0] == small > 0 and res["branches"][0] == 0
     assert res["packed"][1] == res["branches"][1] and res["packed"][2] == res["branches"][2]
     for (xa, ya), (xb, yb) in zip(res["packed"][3], res["branches"][3]):
