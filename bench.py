@@ -577,8 +577,8 @@ def serve_section(args, device, world=1, rank=0):
     from reda_erplacer_gb300.serving import Server, run_stream
     specs = R.design.batch_specs(count=args.serve_jobs, seed=9000, min_cells=5000, max_cells=500000)
     pilot = [R.design.batch_job(*sp) for sp in specs[: min(32, len(specs))]]
-    # the server replays a graph per job, so its capacity is gauged with a batch
-    # of one branch per instance, not with the packed launches
+    # the server runs a graph per job, so its capacity is gauged with a batch of
+    # one branch per instance, not with the batches' packed launches
     os.environ["ERP_BATCH_FORM"] = "branches"
     try:
         bt = R.Batch([d for d, _ in pilot], [b for _, b in pilot], 1.0, start_mode=1, device=device)

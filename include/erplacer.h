@@ -303,10 +303,13 @@ erp_status erp_batch_packed(const erp_batch *b, int32_t *packed_instances);
  * Jobs are submitted as they arrive and wait in a FIFO queue.  Each
  * erp_server_pump round admits queued jobs while their device footprint fits
  * the HBM budget (and the active-job cap), runs `chunk` iterations of every
- * active job in one batched graph (re-captured when the active set changes),
- * and retires jobs whose overflow <= stop_overflow or whose iteration budget is
- * spent, freeing their memory for the next admissions.  Times are seconds on
- * the server's steady clock. */
+ * active job -- each job replays its own captured step graph on its own stream;
+ * with the environment variable ERP_SERVER_FORM=packed, four or more active
+ * jobs of the kind batches pack run as one graph of packed launches instead,
+ * rebuilt when that set changes -- and retires jobs whose overflow <=
+ * stop_overflow or whose iteration budget is spent, freeing their memory for
+ * the next admissions.  Results are each job's alone, bit for bit, in either
+ * form.  Times are seconds on the server's steady clock. */
 typedef struct erp_server_params {
     int32_t device;
     int32_t max_active;         /* jobs on the GPU at once (1: one job at a time) */

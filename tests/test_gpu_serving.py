@@ -18,12 +18,24 @@ def _jobs(R, count, seed):
     return [(d, b) for d, b in mix]
 
 
-def test_server_results_equal_alone(R):
+@pytest.mark.parametrize("form", ["branches", "packed"])
+@pytest.mark.parametrize("max_active,count", [(4, 8), (6, 12)])
+def test_server_results_equal_alone(R, max_active, count, form):
+    """Each job runs its own graph (the default), or, with ERP_SERVER_FORM=packed,
+    a round runs the four or more small jobs active as one graph of packed
+    launches, rebuilt as the set changes (fewer: each its own graph); jobs then
+    move between the two forms as others arrive and retire."""
+    import os
     from reda_erplacer_gb300.serving import Server, run_stream
-    jobs = _jobs(R, 8, seed=91)
-    arrivals = np.array([0.0, 0.0, 0.01, 0.02, 0.05, 0.05, 0.10, 0.12])
-    sv = Server(max_active=4, hbm_budget_gb=8.0, max_iterations=120, stop_overflow=0.5, chunk=8,
-                keep_positions=True)
+    jobs = _jobs(R, count, seed=91)
+    arrivals = np.sort(np.random.default_rng(count).uniform(0.0, 0.15, count))
+    arrivals[:2] = 0.0
+    os.environ["ERP_SERVER_FORM"] = form
+    try:
+        sv = Server(max_active=max_active, hbm_budget_gb=8.0, max_iterations=120, stop_overflow=0.5, chunk=8,
+                    keep_positions=True)
+    finally:
+        del os.environ["ERP_SERVER_FORM"]
     res = run_stream(sv, jobs, arrivals)
     assert len(res) == len(jobs) and all(r["status"] == 0 for r in res)
     # work of different jobs overlapped: some job was admitted before another finished
