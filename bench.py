@@ -687,6 +687,32 @@ def phase_state(args):
     return 0
 
 
+def batch_only(args):
+    """--batch-only NAME: build one batch (NAME "mix": the 64-design mix; "tiny_mix":
+    64 designs of 2,000-4,000 cells on 64^2 bins) in the form the environment
+    variable ERP_BATCH_FORM names, run it to 600 iterations or overflow <= 0.10,
+    print its time and exit: a profiler's view of the batched launches alone."""
+    import torch
+    import __graft_entry__ as G
+    G.build_product()
+    import reda_erplacer_gb300 as R
+    if args.batch_only == "mix":
+        jobs = R.workload_batch(count=64)
+    else:
+        jobs = R.workload_batch(count=64, seed=4100, min_cells=2000, max_cells=4000)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b = R.Batch([d for d, _ in jobs], [x for _, x in jobs], 1.0, start_mode=1)
+    its, _ = b.run(args.batch_iters, stop_overflow=0.10)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    print(json.dumps({"batch": args.batch_only, "form": os.environ.get("ERP_BATCH_FORM", "packed"),
+                      "instances": len(jobs), "packed_instances": b.packed_instances(),
+                      "iterations_total": int(sum(its)), "s": dt}), flush=True)
+    b.close()
+    return 0
+
+
 def run_ours(args):
     world, rank, local = dist_setup()
     import numpy as np
@@ -949,9 +975,14 @@ def main():
                     help="restore the workload from the checkpoint at PATH, run 16 steps (the scatter order "
                          "follows the cells), launch every stage alone twice (erp_profile_stages, one timed "
                          "launch after one untimed) and exit: a profiler's view of one phase of the run")
+    ap.add_argument("--batch-only", choices=["mix", "tiny_mix"], default=None,
+                    help="run one batch (the 64-design mix or 64 tiny designs) in the form "
+                         "ERP_BATCH_FORM names and exit: a profiler's view of the batched launches")
     args = ap.parse_args()
     if args.save_state or args.profile_state:
         return phase_state(args)
+    if args.batch_only:
+        return batch_only(args)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

@@ -209,16 +209,18 @@ class Batch:
     see erp_batch_* in include/erplacer.h."""
 
     def __init__(self, designs, num_bins, target_density=1.0, start_mode=L.START_CENTER, device=0,
-                 precision=L.PREC_FP32):
-        """precision: one erp_precision for every design, or one per design."""
+                 precision=L.PREC_FP32, flags=0):
+        """precision, flags: one value for every design, or one per design."""
         self.lib = L.load()
         K = len(designs)
         self._structs = [d.to_struct() for d in designs]
         darr = (L.Design * K)(*self._structs)
         bins = num_bins if isinstance(num_bins[0], (tuple, list)) else [num_bins] * K
         precs = list(precision) if isinstance(precision, (tuple, list)) else [precision] * K
+        flg = list(flags) if isinstance(flags, (tuple, list)) else [flags] * K
         parr = (L.Params * K)(*[L.Params(int(b[0]), int(b[1]), float(target_density), int(start_mode),
-                                         int(pr), int(device), None, 0) for b, pr in zip(bins, precs)])
+                                         int(pr), int(device), None, int(f))
+                                for b, pr, f in zip(bins, precs, flg)])
         h = C.c_void_p()
         st = self.lib.erp_batch_create(darr, parr, K, C.byref(h))
         L.check(st, None)
