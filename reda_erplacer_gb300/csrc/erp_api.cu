@@ -1164,6 +1164,8 @@ struct erp_batch {
     std::vector<std::pair<int, float>> spec_tuning;   // (candidate, ms of all instances' spectral passes)
     cudaGraphExec_t graph = nullptr;
     bool graph_ready = false;
+    cudaGraphExec_t sort_graph = nullptr;  // the active instances' scatter-order refreshes, a branch each
+    bool sort_ready = false;
     int graph_kernels = 0;
     DevState **d_states = nullptr;   // device array of the instances' state pointers
     int32_t *d_done = nullptr;
@@ -1543,6 +1545,10 @@ static erp_status batch_graph(erp_batch *b, const std::vector<char> &active) {
         cudaGraphExecDestroy(b->graph);
         b->graph_ready = false;
     }
+    if (b->sort_ready) {
+        cudaGraphExecDestroy(b->sort_graph);
+        b->sort_ready = false;
+    }
     std::vector<Ctx *> xs;
     std::vector<char> branch(b->ctx.size(), 0);
     for (size_t i = 0; i < b->ctx.size(); ++i) {
@@ -1587,13 +1593,34 @@ static erp_status batch_graph(erp_batch *b, const std::vector<char> &active) {
         e = cudaGraphInstantiate(&b->graph, g, 0);
         cudaGraphDestroy(g);
     }
+    if (e == cudaSuccess) b->graph_ready = true;
+    // The scatter-order refreshes of the same instances, each on its own stream:
+    // four operations per instance that would otherwise run one after another on
+    // the master stream before every chunk of steps.
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(b->master, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaEventRecord(fork, b->master);
+        for (size_t i = 0; i < b->ctx.size(); ++i) {
+            if (!active[i]) continue;
+            Ctx &c = b->ctx[i]->c;
+            cudaStreamWaitEvent(c.stream, fork, 0);
+            launch_scatter_order(c, c.stream);
+            cudaEventRecord(joins[i], c.stream);
+            cudaStreamWaitEvent(b->master, joins[i], 0);
+        }
+        e = cudaStreamEndCapture(b->master, &g);
+        if (e == cudaSuccess) {
+            e = cudaGraphInstantiate(&b->sort_graph, g, 0);
+            cudaGraphDestroy(g);
+        }
+    }
+    if (e == cudaSuccess) b->sort_ready = true;
     cudaEventDestroy(fork);
     for (auto &j : joins) cudaEventDestroy(j);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return batch_fail(b, ERP_ECUDA, std::string("batch graph: ") + cudaGetErrorString(e));
     }
-    b->graph_ready = true;
     return ERP_OK;
 }
 
@@ -1637,8 +1664,23 @@ extern "C" erp_status erp_batch_run(erp_batch *b, int32_t max_iterations, float 
     erp_status rs = ERP_OK;
     while (n_active > 0 && launched < max_iterations) {
         const int k = std::min(chunk, max_iterations - launched);
-        for (int i = 0; i < K; ++i)
-            if (active[i]) refresh_scatter_order(b->ctx[i]->c, k, b->master);
+        // every active instance's scatter order when one of them is due (an early
+        // refresh changes no result, only which block adds a contribution)
+        bool due = false;
+        for (int i = 0; i < K; ++i) {
+            if (!active[i]) continue;
+            Ctx &c = b->ctx[i]->c;
+            c.sort_age += k;
+            due = due || c.sort_age >= kSortEvery;
+        }
+        if (due) {
+            if (cudaGraphLaunch(b->sort_graph, b->master) != cudaSuccess) {
+                rs = batch_fail(b, ERP_ECUDA, "scatter-order graph launch failed");
+                break;
+            }
+            for (int i = 0; i < K; ++i)
+                if (active[i]) b->ctx[i]->c.sort_age = 0;
+        }
         for (int i = 0; i < k && rs == ERP_OK; ++i)
             if (cudaGraphLaunch(b->graph, b->master) != cudaSuccess)
                 rs = batch_fail(b, ERP_ECUDA, "batch graph launch failed");
@@ -1709,6 +1751,7 @@ extern "C" void erp_batch_destroy(erp_batch *b) {
     cudaSetDevice(b->device);
     if (b->master) cudaStreamSynchronize(b->master);
     if (b->graph_ready) cudaGraphExecDestroy(b->graph);
+    if (b->sort_ready) cudaGraphExecDestroy(b->sort_graph);
     for (auto *c : b->ctx) erp_destroy(c);
     if (b->master) cudaStreamDestroy(b->master);
     if (b->d_states) cudaFree(b->d_states);
