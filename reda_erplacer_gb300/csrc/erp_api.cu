@@ -56,6 +56,48 @@ extern "C" const char *erp_last_error(const erp_ctx *ctx) {
 
 extern "C" int32_t erp_abi_version(void) { return ERP_ABI_VERSION; }
 
+namespace erp {
+// The contexts' arrays come from one stream-ordered pool per device that keeps
+// up to kPoolKeep bytes of freed memory for the next contexts (the device's
+// default pool returns freed memory to the system at every synchronisation), so
+// the next batch or a server admission after a retirement reuses the memory of
+// the contexts that went before instead of mapping it again.
+constexpr unsigned long long kPoolKeep = 8ull << 30;
+
+cudaError_t ctx_alloc(void **p, size_t bytes, cudaStream_t s) {
+    static std::mutex mu;
+    static std::vector<cudaMemPool_t> pools;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    cudaMemPool_t pool = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if ((size_t)dev >= pools.size()) pools.resize((size_t)dev + 1, nullptr);
+        if (!pools[dev]) {
+            cudaMemPoolProps props;
+            memset(&props, 0, sizeof props);
+            props.allocType = cudaMemAllocationTypePinned;
+            props.handleTypes = cudaMemHandleTypeNone;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            cudaMemPool_t np = nullptr;
+            e = cudaMemPoolCreate(&np, &props);
+            if (e != cudaSuccess) return e;
+            unsigned long long keep = kPoolKeep;
+            e = cudaMemPoolSetAttribute(np, cudaMemPoolAttrReleaseThreshold, &keep);
+            if (e != cudaSuccess) {
+                cudaMemPoolDestroy(np);
+                return e;
+            }
+            pools[dev] = np;
+        }
+        pool = pools[dev];
+    }
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+}  // namespace erp
+
 namespace {
 
 bool pow2_ok(int v) { return v >= 16 && v <= 4096 && (v & (v - 1)) == 0; }
@@ -63,10 +105,26 @@ bool pow2_ok(int v) { return v >= 16 && v <= 4096 && (v & (v - 1)) == 0; }
 // Stream-ordered allocations on the context's stream: creating or destroying a
 // context never synchronises the device, so jobs can be admitted and retired
 // while other contexts' work runs.
-template <typename T>
-cudaError_t dalloc(T **p, size_t count, cudaStream_t s) {
-    return cudaMallocAsync((void **)p, sizeof(T) * (count ? count : 1), s);
-}
+// Every array of a context in one pool allocation, each at a 256-byte
+// boundary.  Fifty pool operations per context became one; the pool's time per
+// operation grew with the allocations and frees of earlier contexts, and a
+// batch of 64 small designs created after another in the same process took
+// 80-89 ms, 11.5 ms now (with fixed tile shapes; 20 ms with the autotuning).
+struct ArenaPlan {
+    std::vector<std::pair<void **, size_t>> items;   // (pointer, offset)
+    size_t total = 0;
+    template <typename T>
+    void add(T **p, size_t count) {
+        items.emplace_back(reinterpret_cast<void **>(p), total);
+        total += (sizeof(T) * (count ? count : 1) + 255) & ~size_t(255);
+    }
+    cudaError_t commit(void **base, cudaStream_t s) {
+        const cudaError_t e = ctx_alloc(base, total ? total : 256, s);
+        if (e != cudaSuccess) return e;
+        for (auto &it : items) *it.first = static_cast<char *>(*base) + it.second;
+        return cudaSuccess;
+    }
+};
 
 cudaError_t upload(void *dst, const void *src, size_t bytes, cudaStream_t s) {
     if (!bytes) return cudaSuccess;
@@ -91,15 +149,16 @@ erp_status check_device(int dev, std::string &err) {
         err = "device ordinal out of range";
         return ERP_EINVAL;
     }
-    cudaDeviceProp prop;
-    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
-        err = "cudaGetDeviceProperties failed";
+    int major = 0, minor = 0;   // two attributes, not the whole property set (milliseconds per call)
+    if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess) {
+        cudaGetLastError();
+        err = "cudaDeviceGetAttribute failed";
         return ERP_ECUDA;
     }
-    if (prop.major != 10 || prop.minor != 3) {
+    if (major != 10 || minor != 3) {
         char buf[128];
-        snprintf(buf, sizeof buf, "device %d is sm_%d%d; this library is built for sm_103a only", dev,
-                 prop.major, prop.minor);
+        snprintf(buf, sizeof buf, "device %d is sm_%d%d; this library is built for sm_103a only", dev, major, minor);
         err = buf;
         return ERP_ENODEV;
     }
@@ -107,6 +166,29 @@ erp_status check_device(int dev, std::string &err) {
         err = "cudaSetDevice failed";
         return ERP_ECUDA;
     }
+    return ERP_OK;
+}
+
+// The kernels' shared-memory attributes and the resident block counts that size
+// the streaming grids belong to the device (its primary context), so they are
+// set once per device and process, not per context: a batch creates its
+// contexts on several threads at once.  (cudaDeviceReset after the first
+// context on a device is not supported: it would clear the attributes.)
+erp_status prepare_device(int dev, std::string &err) {
+    static std::mutex mu;
+    static std::vector<char> ready;
+    std::lock_guard<std::mutex> lock(mu);
+    if ((size_t)dev < ready.size() && ready[dev]) return ERP_OK;
+    cudaError_t e = spectral_prepare();
+    if (e == cudaSuccess) e = place_prepare();
+    if (e == cudaSuccess) e = place_occupancy();
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        err = std::string("kernel set-up: ") + cudaGetErrorString(e);
+        return ERP_ECUDA;
+    }
+    if ((size_t)dev >= ready.size()) ready.resize((size_t)dev + 1, 0);
+    ready[dev] = 1;
     return ERP_OK;
 }
 
@@ -161,16 +243,9 @@ erp_status validate(const erp_design *d, std::string &err) {
 }
 
 void free_ctx(Ctx &c) {
-    void *ptrs[] = {c.x, c.y, c.xy, c.w, c.h, c.npins, c.cw, c.ch, c.offx, c.offy, c.ratio, c.wlgx, c.wlgy,
-                    c.dgp, c.pos, c.prev_x, c.prev_y, c.prev_gx, c.prev_gy, c.slot_cell, c.slot_off,
-                    c.slot_grad, c.net_ptr, c.net_hpwl, c.cell_slot_ptr, c.cell_slots, c.dmap,
-                    c.initial, c.rho, c.t1, c.tx, c.ty, c.tp, c.fx, c.fy, c.psi, c.tw_m, c.tw_n,
-                    c.ek_m, c.ek_n, c.wu, c.wv, c.partials, c.st, c.perm, c.skey, c.soff, c.sratio,
-                    c.sort_key, c.sort_rank, c.sort_hist, c.sort_start};
-    for (void *p : ptrs) {   // stream-ordered, on the stream they were allocated on
-        if (!p) continue;
-        if (c.stream) cudaFreeAsync(p, c.stream);
-        else cudaFree(p);
+    if (c.arena) {   // stream-ordered, on the stream it was allocated on
+        if (c.stream) cudaFreeAsync(c.arena, c.stream);
+        else cudaFree(c.arena);
     }
     if (c.h_st) cudaFreeHost(c.h_st);
     if (c.gemm) dctgemm_destroy(c.gemm);   // synchronises the stream before freeing
@@ -273,9 +348,8 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     s = check_device(prm.device, c.err);
     if (s != ERP_OK) return s;
     c.device = prm.device;
-    CK(spectral_prepare());
-    CK(place_prepare());
-    CK(place_occupancy());
+    s = prepare_device(c.device, c.err);
+    if (s != ERP_OK) return s;
     const int N = d->num_nodes, NM = d->num_movable, P = d->num_pins, E = d->num_nets;
     c.N = N; c.NM = NM; c.P = P; c.E = E; c.NS = P;
     c.m = prm.num_bins_x; c.n = prm.num_bins_y;
@@ -405,34 +479,41 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     const size_t mn = (size_t)c.m * c.n;
     float **cellarr[] = {&c.x, &c.y, &c.w, &c.h, &c.npins, &c.cw, &c.ch, &c.offx, &c.offy, &c.ratio,
                          &c.wlgx, &c.wlgy, &c.prev_x, &c.prev_y, &c.prev_gx, &c.prev_gy};
-    cudaStream_t s0 = c.stream;
-    for (float **a : cellarr) CK(dalloc(a, (size_t)N + 4, s0));
-    CK(dalloc(&c.xy, (size_t)N + 4, s0));
-    CK(dalloc(&c.slot_cell, P, s0));
-    CK(dalloc(&c.slot_off, P, s0));
-    CK(dalloc(&c.slot_grad, P, s0));
-    CK(dalloc(&c.net_ptr, (size_t)E + 1, s0));
-    CK(dalloc(&c.net_hpwl, E, s0));
-    CK(dalloc(&c.cell_slot_ptr, (size_t)NM + 1, s0));
-    CK(dalloc(&c.cell_slots, hcell_slots.size(), s0));
-    CK(dalloc(&c.perm, NM, s0));
-    CK(dalloc(&c.pos, (size_t)NM + 4, s0));
-    CK(dalloc(&c.dgp, (size_t)NM + 4, s0));
-    CK(dalloc(&c.skey, NM, s0));
-    CK(dalloc(&c.soff, NM, s0));
-    CK(dalloc(&c.sratio, NM, s0));
-    CK(dalloc(&c.sort_key, NM, s0));
-    CK(dalloc(&c.sort_rank, NM, s0));
-    CK(dalloc(&c.sort_hist, scatter_tiles(c.m, c.n), s0));
-    CK(dalloc(&c.sort_start, scatter_tiles(c.m, c.n), s0));
-    CK(dalloc(&c.dmap, mn, s0));
+    ArenaPlan ap;
+    for (float **a : cellarr) ap.add(a, (size_t)N + 4);
+    ap.add(&c.xy, (size_t)N + 4);
+    ap.add(&c.slot_cell, P);
+    ap.add(&c.slot_off, P);
+    ap.add(&c.slot_grad, P);
+    ap.add(&c.net_ptr, (size_t)E + 1);
+    ap.add(&c.net_hpwl, E);
+    ap.add(&c.cell_slot_ptr, (size_t)NM + 1);
+    ap.add(&c.cell_slots, hcell_slots.size());
+    ap.add(&c.perm, NM);
+    ap.add(&c.pos, (size_t)NM + 4);
+    ap.add(&c.dgp, (size_t)NM + 4);
+    ap.add(&c.skey, NM);
+    ap.add(&c.soff, NM);
+    ap.add(&c.sratio, NM);
+    ap.add(&c.sort_key, NM);
+    ap.add(&c.sort_rank, NM);
+    ap.add(&c.sort_hist, scatter_tiles(c.m, c.n));
+    ap.add(&c.sort_start, scatter_tiles(c.m, c.n));
+    ap.add(&c.dmap, mn);
     float **maps[] = {&c.initial, &c.rho, &c.t1, &c.tx, &c.ty, &c.tp, &c.fx, &c.fy, &c.psi};
-    for (float **a : maps) CK(dalloc(a, mn, s0));
-    CK(dalloc(&c.partials, kMaxPartials, s0));
+    for (float **a : maps) ap.add(a, mn);
+    ap.add(&c.partials, kMaxPartials);
     c.max_partials = kMaxPartials;
-    CK(dalloc(&c.st, 1, s0));
+    ap.add(&c.st, 1);
+    ap.add(&c.tw_m, (size_t)c.m / 2);
+    ap.add(&c.tw_n, (size_t)c.n / 2);
+    ap.add(&c.ek_m, c.m);
+    ap.add(&c.ek_n, c.n);
+    ap.add(&c.wu, c.m);
+    ap.add(&c.wv, c.n);
+    CK(ap.commit(&c.arena, c.stream));
     CK(cudaMallocHost((void **)&c.h_st, sizeof(DevState)));
-    spectral_tables(c.m, c.n, c.bin_w, c.bin_h, &c.tw_m, &c.tw_n, &c.ek_m, &c.ek_n, &c.wu, &c.wv, c.stream);
+    spectral_tables_fill(c.m, c.n, c.bin_w, c.bin_h, c.tw_m, c.tw_n, c.ek_m, c.ek_n, c.wu, c.wv, c.stream);
     CK(cudaGetLastError());
     if (prm.precision != ERP_PREC_FP32) {
         c.gemm = dctgemm_create(c.m, c.n, c.bin_w, c.bin_h, prm.precision == ERP_PREC_TF32_GEMM ? 0 : 1, c.stream,

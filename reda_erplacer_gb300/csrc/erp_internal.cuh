@@ -130,6 +130,7 @@ struct Ctx {
     int32_t max_partials;
     DevState *st;
     DevState *h_st;            // pinned host mirror
+    void *arena;               // the one allocation that holds every device array above
     DctGemmPlan *gemm;         // tensor-core spectral solve (precision TF32 / BF16x3), else nullptr
     // --- graph ---
     cudaGraphExec_t graph;
@@ -210,6 +211,10 @@ enum PackKind { PK_WA, PK_GATHER, PK_SCATTER, PK_ROWS_DCT_W, PK_COLS_W, PK_ROWS_
 void packed_place_stage(PackKind k, const std::vector<Ctx *> &xs, PackedArena &ar, std::vector<PackedLaunch> &out);
 bool packed_place_launch(const PackedLaunch &l, const unsigned char *dev, cudaStream_t s);
 
+// A stream-ordered allocation for a context's arrays, from the library's pool on
+// the current device (freed with cudaFreeAsync; erp_api.cu).
+cudaError_t ctx_alloc(void **p, size_t bytes, cudaStream_t s);
+
 // spectral engine for the standalone solve
 // The sequences-per-block alternatives of the warp-form spectral passes (sides
 // 64..256) that a batch's autotuner times against the fixed shape (four).
@@ -229,6 +234,9 @@ struct SpectralPlan {
 };
 void spectral_tables(int m, int n, float bin_w, float bin_h, float2 **tw_m, float2 **tw_n,
                      float2 **ek_m, float2 **ek_n, float **wu, float **wv, cudaStream_t s);
+// The same tables into arrays the caller allocated (m / 2, n / 2, m, n, m, n elements).
+void spectral_tables_fill(int m, int n, float bin_w, float bin_h, float2 *tw_m, float2 *tw_n, float2 *ek_m,
+                          float2 *ek_n, float *wu, float *wv, cudaStream_t s);
 struct SpectralArgs {
     const float *rho_in = nullptr;          // standalone: rho given directly
     unsigned long long *dmap = nullptr;     // loop: int64 fixed-point movable map

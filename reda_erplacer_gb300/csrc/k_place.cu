@@ -1392,8 +1392,8 @@ void launch_initial_density(Ctx &c, const float *, const float *, const float *,
             hcy[i] = (l + hh) / 2.0f;
         }
         float *dcx, *dcy;
-        cudaMallocAsync(&dcx, sizeof(float) * c.m, c.stream);
-        cudaMallocAsync(&dcy, sizeof(float) * c.n, c.stream);
+        ctx_alloc((void **)&dcx, sizeof(float) * c.m, c.stream);
+        ctx_alloc((void **)&dcy, sizeof(float) * c.n, c.stream);
         cudaMemcpyAsync(dcx, hcx, sizeof(float) * c.m, cudaMemcpyHostToDevice, c.stream);
         cudaMemcpyAsync(dcy, hcy, sizeof(float) * c.n, cudaMemcpyHostToDevice, c.stream);
         k_initial_density<<<count < 4096 ? count : 4096, kThreads, 0, c.stream>>>(

@@ -1125,10 +1125,12 @@ constexpr int kRowPairs = 2;
 
 static int col_pairs(int m) { return m <= 2048 ? 4 : 2; }
 
-void spectral_tables(int m, int n, float bin_w, float bin_h, float2 **tw_m, float2 **tw_n,
-                     float2 **ek_m, float2 **ek_n, float **wu, float **wv, cudaStream_t s) {
+// Host-computed tables (FP64 angles rounded to FP32) uploaded to the given
+// arrays; pageable copies, so the host buffers can go as soon as the calls return.
+void spectral_tables_fill(int m, int n, float bin_w, float bin_h, float2 *tw_m, float2 *tw_n, float2 *ek_m,
+                          float2 *ek_n, float *wu, float *wv, cudaStream_t s) {
     auto tw = [](int N) {
-        float2 *h = new float2[N / 2];
+        std::vector<float2> h(N / 2);
         for (int k = 0; k < N / 2; ++k) {
             double a = -2.0 * 3.14159265358979323846 * (double)k / (double)N;
             h[k] = make_float2((float)cos(a), (float)sin(a));
@@ -1136,34 +1138,38 @@ void spectral_tables(int m, int n, float bin_w, float bin_h, float2 **tw_m, floa
         return h;
     };
     auto ek = [](int N) {
-        float2 *h = new float2[N];
+        std::vector<float2> h(N);
         for (int k = 0; k < N; ++k) {
             double a = 3.14159265358979323846 * (double)k / (2.0 * N);
             h[k] = make_float2((float)cos(a), (float)-sin(a));
         }
         return h;
     };
-    float2 *h_twm = tw(m), *h_twn = tw(n), *h_ekm = ek(m), *h_ekn = ek(n);
-    float *h_wu = new float[m], *h_wv = new float[n];
+    const std::vector<float2> h_twm = tw(m), h_twn = tw(n), h_ekm = ek(m), h_ekn = ek(n);
+    std::vector<float> h_wu(m), h_wv(n);
     const float tpm = (float)(2.0 * 3.14159265358979323846) / (float)m;
     for (int i = 0; i < m; ++i) h_wu[i] = (float)i * tpm;
     const float wv_div = bin_w / bin_h;
     const float tpn = (float)(2.0 * 3.14159265358979323846) / (float)n;
     for (int j = 0; j < n; ++j) h_wv[j] = ((float)j * tpn) * wv_div;
-    cudaMallocAsync(tw_m, sizeof(float2) * (m / 2), s);
-    cudaMallocAsync(tw_n, sizeof(float2) * (n / 2), s);
-    cudaMallocAsync(ek_m, sizeof(float2) * m, s);
-    cudaMallocAsync(ek_n, sizeof(float2) * n, s);
-    cudaMallocAsync(wu, sizeof(float) * m, s);
-    cudaMallocAsync(wv, sizeof(float) * n, s);
-    cudaMemcpyAsync(*tw_m, h_twm, sizeof(float2) * (m / 2), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(*tw_n, h_twn, sizeof(float2) * (n / 2), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(*ek_m, h_ekm, sizeof(float2) * m, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(*ek_n, h_ekn, sizeof(float2) * n, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(*wu, h_wu, sizeof(float) * m, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(*wv, h_wv, sizeof(float) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(tw_m, h_twm.data(), sizeof(float2) * (m / 2), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(tw_n, h_twn.data(), sizeof(float2) * (n / 2), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(ek_m, h_ekm.data(), sizeof(float2) * m, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(ek_n, h_ekn.data(), sizeof(float2) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(wu, h_wu.data(), sizeof(float) * m, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(wv, h_wv.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s);
+}
+
+void spectral_tables(int m, int n, float bin_w, float bin_h, float2 **tw_m, float2 **tw_n,
+                     float2 **ek_m, float2 **ek_n, float **wu, float **wv, cudaStream_t s) {
+    ctx_alloc((void **)tw_m, sizeof(float2) * (m / 2), s);
+    ctx_alloc((void **)tw_n, sizeof(float2) * (n / 2), s);
+    ctx_alloc((void **)ek_m, sizeof(float2) * m, s);
+    ctx_alloc((void **)ek_n, sizeof(float2) * n, s);
+    ctx_alloc((void **)wu, sizeof(float) * m, s);
+    ctx_alloc((void **)wv, sizeof(float) * n, s);
+    spectral_tables_fill(m, n, bin_w, bin_h, *tw_m, *tw_n, *ek_m, *ek_n, *wu, *wv, s);
     cudaStreamSynchronize(s);
-    delete[] h_twm; delete[] h_twn; delete[] h_ekm; delete[] h_ekn; delete[] h_wu; delete[] h_wv;
 }
 
 constexpr int kRowWarps = 4;   // rows per block, warp kernels
