@@ -1600,20 +1600,22 @@ static void pack_launch(const std::vector<PackedLaunch> &ls, const void *dev_are
 }
 
 // The packed launches of one step over xs, with their argument tables uploaded
-// to the batch's device buffer.
+// to the batch's device buffer in the master stream's order: the graph launches
+// already queued read the old tables, the ones after this call the new ones, and
+// the host does not wait for the queued work.
 static erp_status batch_pack_plan(erp_batch *b, const std::vector<Ctx *> &xs, std::vector<PackedLaunch> &ls) {
     PackedArena ar;
     pack_plan(xs, ar, ls);
     if (ar.host.size() > b->pack_cap) {
-        if (b->pack_dev) cudaFree(b->pack_dev);
+        if (b->pack_dev) cudaFreeAsync(b->pack_dev, b->master);
         b->pack_dev = nullptr;
         b->pack_cap = 0;
-        if (cudaMalloc(&b->pack_dev, ar.host.size()) != cudaSuccess)
+        if (cudaMallocAsync(&b->pack_dev, ar.host.size(), b->master) != cudaSuccess)
             return batch_fail(b, ERP_ENOMEM, "packed argument tables: allocation failed");
         b->pack_cap = ar.host.size();
     }
-    if (!ar.host.empty() &&
-        cudaMemcpy(b->pack_dev, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    if (!ar.host.empty() && cudaMemcpyAsync(b->pack_dev, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice,
+                                            b->master) != cudaSuccess)
         return batch_fail(b, ERP_ECUDA, "packed argument tables: upload failed");
     return ERP_OK;
 }
@@ -1783,8 +1785,9 @@ extern "C" erp_status erp_batch_run(erp_batch *b, int32_t max_iterations, float 
                 for (int i = 0; i < K; ++i)
                     if (b->h_done[pending * K + i]) active[i] = 0;
                 n_active = now;
+                // captured while the chunk in flight runs on: its graphs are freed when
+                // it completes, and the new tables reach the device in stream order
                 if (n_active > 0) {
-                    cudaStreamSynchronize(b->master);
                     rs = batch_graph(b, active);
                     if (rs != ERP_OK) break;
                 }
