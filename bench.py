@@ -564,31 +564,33 @@ class LazyJobs:
 
 def serve_section(args, device, world=1, rank=0):
     """Serving workload: an open-loop stream of jobs (cells log-uniform 5k-500k,
-    each its own seed) with Poisson arrivals at 80 % of the capacity measured by
-    a batched pilot run; admission under a 150 GB HBM budget, retire at overflow
-    <= 0.10 or 600 iterations.  p50/p99 completion latency and jobs/hour of the
+    each its own seed) with Poisson arrivals at 80 % of the server's measured
+    capacity; admission under a 150 GB HBM budget, retire at overflow <= 0.10 or
+    600 iterations.  p50/p99 completion latency and jobs/hour of the
     continuous-batching server, and of the same stream served one job at a
-    time.  With several ranks each GPU runs its own server, the capacity is the
-    sum of the ranks' pilots and each arriving job is routed to the rank with
-    the least assigned work (host-side dispatch, no collective)."""
+    time.  The capacity is that of the same server (same limits) overloaded by
+    the stream's first 256 jobs arriving at 200 per second: its steady completion
+    rate, the middle half of the completions over the time they took (the ramp
+    and the tail, where the GPU is not full, left out); set-up and admission are
+    inside it.  With several ranks each GPU runs
+    its own server, the capacity is the sum of the ranks' pilots and each
+    arriving job is routed to the rank with the least assigned work (host-side
+    dispatch, no collective)."""
     import numpy as np
     import reda_erplacer_gb300 as R
     from reda_erplacer_gb300.dispatch import job_cost, route_stream
     from reda_erplacer_gb300.serving import Server, run_stream
     specs = R.design.batch_specs(count=args.serve_jobs, seed=9000, min_cells=5000, max_cells=500000)
-    pilot = [R.design.batch_job(*sp) for sp in specs[: min(32, len(specs))]]
-    # the server runs a graph per job, so its capacity is gauged with a batch of
-    # one branch per instance, not with the batches' packed launches
-    os.environ["ERP_BATCH_FORM"] = "branches"
-    try:
-        bt = R.Batch([d for d, _ in pilot], [b for _, b in pilot], 1.0, start_mode=1, device=device)
-    finally:
-        del os.environ["ERP_BATCH_FORM"]
-    t0 = time.perf_counter()
-    bt.run(args.batch_iters, stop_overflow=0.10)
-    cap = allreduce_sum(len(pilot) / (time.perf_counter() - t0), world)
-    bt.close()
-    del pilot
+    n_pilot = min(256, len(specs))
+    pilot = LazyJobs(specs[:n_pilot])
+    sv = Server(max_active=64, hbm_budget_gb=150.0, max_iterations=args.batch_iters, stop_overflow=0.10, chunk=8,
+                device=device)
+    res = run_stream(sv, pilot, np.arange(n_pilot) / 200.0)
+    sv.close()
+    pilot.close()
+    fin = np.sort([r["finish_s"] for r in res])
+    q1, q3 = len(fin) // 4, (3 * len(fin)) // 4
+    cap = allreduce_sum((q3 - q1) / max(fin[q3] - fin[q1], 1e-9), world)
     rate = 0.8 * cap
     rng = np.random.default_rng(17)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(specs)))
