@@ -126,7 +126,12 @@ int32_t erp_abi_version(void);
 
 /* Placement::new (src/placement.rs:159-178): Bins::new, PlacementSolution::new,
  * PotentialComputation::new (incl. the fixed-cell initial density map),
- * HpwlComputation::new, Scheduler::new, Nesterov::new. */
+ * HpwlComputation::new, Scheduler::new, Nesterov::new.
+ * The context's device arrays are one stream-ordered allocation from the
+ * library's own memory pool on the device; erp_destroy returns it to that pool,
+ * which keeps up to 8 GiB of freed memory for later contexts (the rest goes
+ * back to the system).  Not supported: cudaDeviceReset on a device after its
+ * first context (kernel attributes are set once per device and process). */
 erp_status erp_create(const erp_design *design, const erp_params *params, erp_ctx **out);
 void erp_destroy(erp_ctx *ctx);
 
