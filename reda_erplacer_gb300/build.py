@@ -32,7 +32,7 @@ CU_SOURCES = {
 CPP_SOURCES = ["synth.cpp", "lefdef.cpp"]
 CLI_SOURCE = "erplacer_cli.cpp"   # the command-line driver, linked against the library
 HEADERS = ["erp_internal.cuh", "reduce.cuh", "bulk_copy.cuh", "dfloat.h", "fixedpoint.h", "binrange.h",
-           "packed.h"]
+           "packed.h", "arena.h"]
 
 
 def _deps():

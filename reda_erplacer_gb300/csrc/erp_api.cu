@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "erp_internal.cuh"
+#include "arena.h"
 
 using namespace erp;
 
@@ -105,27 +106,6 @@ bool pow2_ok(int v) { return v >= 16 && v <= 4096 && (v & (v - 1)) == 0; }
 // Stream-ordered allocations on the context's stream: creating or destroying a
 // context never synchronises the device, so jobs can be admitted and retired
 // while other contexts' work runs.
-// Every array of a context in one pool allocation, each at a 256-byte
-// boundary.  Fifty pool operations per context became one; the pool's time per
-// operation grew with the allocations and frees of earlier contexts, and a
-// batch of 64 small designs created after another in the same process took
-// 80-89 ms, 11.5 ms now (with fixed tile shapes; 20 ms with the autotuning).
-struct ArenaPlan {
-    std::vector<std::pair<void **, size_t>> items;   // (pointer, offset)
-    size_t total = 0;
-    template <typename T>
-    void add(T **p, size_t count) {
-        items.emplace_back(reinterpret_cast<void **>(p), total);
-        total += (sizeof(T) * (count ? count : 1) + 255) & ~size_t(255);
-    }
-    cudaError_t commit(void **base, cudaStream_t s) {
-        const cudaError_t e = ctx_alloc(base, total ? total : 256, s);
-        if (e != cudaSuccess) return e;
-        for (auto &it : items) *it.first = static_cast<char *>(*base) + it.second;
-        return cudaSuccess;
-    }
-};
-
 cudaError_t upload(void *dst, const void *src, size_t bytes, cudaStream_t s) {
     if (!bytes) return cudaSuccess;
     return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
@@ -511,7 +491,13 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
     ap.add(&c.ek_n, c.n);
     ap.add(&c.wu, c.m);
     ap.add(&c.wv, c.n);
-    CK(ap.commit(&c.arena, c.stream));
+    // Every array in one pool allocation (arena.h).  Fifty pool operations per
+    // context became one; the pool's time per operation grew with the
+    // allocations and frees of earlier contexts, and a batch of 64 small designs
+    // created after another in the same process took 80-89 ms, 11.5 ms now
+    // (fixed tile shapes; 20 ms with the autotuning).
+    CK(ctx_alloc(&c.arena, ap.bytes(), c.stream));
+    ap.place(c.arena);
     CK(cudaMallocHost((void **)&c.h_st, sizeof(DevState)));
     spectral_tables_fill(c.m, c.n, c.bin_w, c.bin_h, c.tw_m, c.tw_n, c.ek_m, c.ek_n, c.wu, c.wv, c.stream);
     CK(cudaGetLastError());
