@@ -58,7 +58,10 @@ extern "C" const char *erp_last_error(const erp_ctx *ctx) {
 extern "C" int32_t erp_abi_version(void) { return ERP_ABI_VERSION; }
 
 namespace erp {
-// The contexts' arrays come from one stream-ordered pool per device that keeps
+// Stream-ordered allocations on the context's stream: creating or destroying a
+// context never synchronises the device, so jobs can be admitted and retired
+// while other contexts' work runs.  The contexts' arrays come from one pool per
+// device that keeps
 // up to kPoolKeep bytes of freed memory for the next contexts (the device's
 // default pool returns freed memory to the system at every synchronisation), so
 // the next batch or a server admission after a retirement reuses the memory of
@@ -103,9 +106,6 @@ namespace {
 
 bool pow2_ok(int v) { return v >= 16 && v <= 4096 && (v & (v - 1)) == 0; }
 
-// Stream-ordered allocations on the context's stream: creating or destroying a
-// context never synchronises the device, so jobs can be admitted and retired
-// while other contexts' work runs.
 cudaError_t upload(void *dst, const void *src, size_t bytes, cudaStream_t s) {
     if (!bytes) return cudaSuccess;
     return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
