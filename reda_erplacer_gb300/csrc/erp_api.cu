@@ -61,11 +61,10 @@ namespace erp {
 // Stream-ordered allocations on the context's stream: creating or destroying a
 // context never synchronises the device, so jobs can be admitted and retired
 // while other contexts' work runs.  The contexts' arrays come from one pool per
-// device that keeps
-// up to kPoolKeep bytes of freed memory for the next contexts (the device's
-// default pool returns freed memory to the system at every synchronisation), so
-// the next batch or a server admission after a retirement reuses the memory of
-// the contexts that went before instead of mapping it again.
+// device that keeps up to kPoolKeep bytes of freed memory for the next contexts
+// (the device's default pool returns freed memory to the system at every
+// synchronisation), so the next batch or a server admission after a retirement
+// reuses the memory of the contexts that went before instead of mapping it again.
 constexpr unsigned long long kPoolKeep = 8ull << 30;
 
 cudaError_t ctx_alloc(void **p, size_t bytes, cudaStream_t s) {
