@@ -710,6 +710,7 @@ def batch_only(args):
     dt = time.perf_counter() - t0
     print(json.dumps({"batch": args.batch_only, "form": os.environ.get("ERP_BATCH_FORM", "packed"),
                       "instances": len(jobs), "packed_instances": b.packed_instances(),
+                      "scatter_cells_per_block": b.tuning()[0], "spectral_seqs_per_block": b.spectral_tuning()[0],
                       "iterations_total": int(sum(its)), "s": dt}), flush=True)
     b.close()
     return 0
