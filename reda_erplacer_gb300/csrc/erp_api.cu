@@ -1275,8 +1275,16 @@ extern "C" erp_status erp_batch_create(const erp_design *designs, const erp_para
     std::vector<erp_status> st(count, ERP_OK);
     std::vector<std::string> msg(count);
     std::atomic<int> next(0);
+    // largest designs first (pins + cells: the host preparation's work), so that
+    // no big one starts last and leaves the other threads idle
+    std::vector<int> order(count);
+    for (int i = 0; i < count; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (int64_t)designs[a].num_pins + designs[a].num_nodes > (int64_t)designs[b].num_pins + designs[b].num_nodes;
+    });
     auto worker = [&]() {
-        for (int i = next++; i < count; i = next++) {
+        for (int k = next++; k < count; k = next++) {
+            const int i = order[k];
             erp_params p;
             memset(&p, 0, sizeof p);
             if (params) p = params[i];
