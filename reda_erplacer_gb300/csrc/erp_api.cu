@@ -16,6 +16,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "erp_internal.cuh"
 #include "arena.h"
 
@@ -58,6 +60,15 @@ extern "C" const char *erp_last_error(const erp_ctx *ctx) {
 extern "C" int32_t erp_abi_version(void) { return ERP_ABI_VERSION; }
 
 namespace erp {
+// A named range on the host timeline of a profiler (NVTX, header-only; no cost
+// without a profiler attached): one per public call that does device work.
+struct HostRange {
+    explicit HostRange(const char *name) { nvtxRangePushA(name); }
+    ~HostRange() { nvtxRangePop(); }
+    HostRange(const HostRange &) = delete;
+    HostRange &operator=(const HostRange &) = delete;
+};
+
 // Stream-ordered allocations on the context's stream: creating or destroying a
 // context never synchronises the device, so jobs can be admitted and retired
 // while other contexts' work runs.  The contexts' arrays come from one pool per
@@ -554,6 +565,7 @@ static erp_status create_impl(const erp_design *d, const erp_params *pp, Ctx &c)
 }
 
 extern "C" erp_status erp_create(const erp_design *design, const erp_params *params, erp_ctx **out) {
+    HostRange range_("erp_create");
     g_create_err.clear();
     if (!out) {
         g_create_err = "out is NULL";
@@ -742,6 +754,7 @@ static erp_status enqueue_step(Ctx &c) {
 }
 
 extern "C" erp_status erp_step(erp_ctx *ctx, erp_step_stats *stats) {
+    HostRange range_("erp_step");
     CTX_CHECK();
     erp_status s = enqueue_step(c);
     if (s != ERP_OK) return s;
@@ -803,6 +816,7 @@ extern "C" erp_status erp_step_host(erp_ctx *ctx, float *x, float *y, erp_step_s
 
 extern "C" erp_status erp_run(erp_ctx *ctx, int32_t max_iterations, float stop_overflow,
                               int32_t *iterations_run, erp_step_stats *last) {
+    HostRange range_("erp_run");
     CTX_CHECK();
     if (max_iterations < 0) return ERP_EINVAL;
     erp_status s = pull_state(c);
@@ -1260,6 +1274,7 @@ static erp_status batch_fail(erp_batch *b, erp_status s, const std::string &msg)
 
 extern "C" erp_status erp_batch_create(const erp_design *designs, const erp_params *params,
                                        int32_t count, erp_batch **out) {
+    HostRange range_("erp_batch_create");
     g_create_err.clear();
     if (!out || !designs || count < 1) {
         g_create_err = "invalid batch arguments";
@@ -1720,6 +1735,7 @@ static erp_status pull_states(erp_batch *b) {
 
 extern "C" erp_status erp_batch_run(erp_batch *b, int32_t max_iterations, float stop_overflow,
                                     int32_t *iterations, erp_step_stats *last) {
+    HostRange range_("erp_batch_run");
     if (!b || max_iterations < 0) return ERP_EINVAL;
     b->err.clear();
     if (cudaSetDevice(b->device) != cudaSuccess) return batch_fail(b, ERP_ECUDA, "cudaSetDevice failed");
@@ -2305,6 +2321,7 @@ static void server_bury(erp_server *sv, uint64_t completed_round) {
 }
 
 extern "C" erp_status erp_server_pump(erp_server *sv, int32_t *active_out, int32_t *queued_out) {
+    HostRange range_("erp_server_pump");
     if (!sv) return ERP_EINVAL;
     sv->err.clear();
     if (cudaSetDevice(sv->p.device) != cudaSuccess) return ERP_ECUDA;
