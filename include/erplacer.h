@@ -34,7 +34,8 @@ typedef enum erp_status {
     ERP_ETIMEDOUT = 5,  /* a bounded device wait ran out */
     ERP_ENOTSUP = 6,    /* feature not supported for these parameters */
     ERP_ENODEV = 7,     /* no CUDA device of compute capability 10.3 */
-    ERP_ESTATE = 8      /* call not valid in the current state */
+    ERP_ESTATE = 8,     /* call not valid in the current state */
+    ERP_ECANCELED = 9   /* the job was cancelled (erp_server_cancel) */
 } erp_status;
 
 /* Placement database, structure-of-arrays + CSR (the fields of reda-db's
@@ -341,6 +342,12 @@ erp_status erp_server_submit(erp_server *s, int64_t job_id, const erp_design *de
                              const erp_params *params);
 /* One scheduling round; reports the active and queued job counts. */
 erp_status erp_server_pump(erp_server *s, int32_t *active, int32_t *queued);
+/* Withdraw a job: a queued one leaves the queue; a running one retires at once
+ * (the iterations already launched for it finish on the device, and its memory
+ * is released when they have); one still being set up retires when the set-up
+ * ends.  Its result carries ERP_ECANCELED and the state it reached.  The other
+ * jobs are not affected.  ERP_EINVAL if no queued or running job has this id. */
+erp_status erp_server_cancel(erp_server *s, int64_t job_id);
 /* Move up to `cap` finished jobs into out[]; *count receives how many. */
 erp_status erp_server_poll(erp_server *s, erp_job_result *out, int32_t cap, int32_t *count);
 /* Final positions of a retired job (keep_positions = 1). */

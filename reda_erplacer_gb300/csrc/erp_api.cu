@@ -49,6 +49,7 @@ extern "C" const char *erp_status_string(erp_status s) {
     case ERP_ENOTSUP: return "not supported";
     case ERP_ENODEV: return "no sm_103 CUDA device";
     case ERP_ESTATE: return "invalid state";
+    case ERP_ECANCELED: return "cancelled";
     }
     return "unknown";
 }
@@ -1937,6 +1938,7 @@ struct Job {
     erp_status prep = ERP_OK;   // outcome of the admission worker's set-up
     int form = -1;              // how its last round ran: -1 none yet, 0 its own branch, 1 packed
     cudaEvent_t ev = nullptr;   // marks its own stream's work when it moves into the packed chain
+    bool cancel = false;        // cancelled while its admission worker set it up
     Job() = default;
     Job(const Job &) = delete;
     Job &operator=(const Job &) = delete;
@@ -2375,8 +2377,8 @@ extern "C" erp_status erp_server_pump(erp_server *sv, int32_t *active_out, int32
                                [&](const std::unique_ptr<Job> &p) { return p.get() == jr; });
         std::unique_ptr<Job> jp = std::move(*it);
         sv->preparing.erase(it);
-        if (jp->prep != ERP_OK) {
-            server_record(sv, *jp, jp->prep);
+        if (jp->prep != ERP_OK || jp->cancel) {
+            server_record(sv, *jp, jp->prep != ERP_OK ? jp->prep : ERP_ECANCELED);
             if (jp->ctx) {
                 std::lock_guard<std::mutex> lk(sv->mu);
                 sv->to_destroy.push_back(jp->ctx);
@@ -2419,6 +2421,40 @@ extern "C" erp_status erp_server_pump(erp_server *sv, int32_t *active_out, int32
     if (active_out) *active_out = (int32_t)(sv->active.size() + sv->preparing.size());
     if (queued_out) *queued_out = (int32_t)(sv->queue.size() - sv->qhead);
     return ERP_OK;
+}
+
+extern "C" erp_status erp_server_cancel(erp_server *sv, int64_t job_id) {
+    if (!sv) return ERP_EINVAL;
+    sv->err.clear();
+    if (cudaSetDevice(sv->p.device) != cudaSuccess) return ERP_ECUDA;
+    for (size_t k = sv->qhead; k < sv->queue.size(); ++k)   // queued: its budget was never taken
+        if (sv->queue[k]->id == job_id) {
+            std::unique_ptr<Job> jp = std::move(sv->queue[k]);
+            sv->queue.erase(sv->queue.begin() + (std::ptrdiff_t)k);
+            server_record(sv, *jp, ERP_ECANCELED);
+            return ERP_OK;
+        }
+    for (size_t k = 0; k < sv->active.size(); ++k)   // running: retired like a finished job
+        if (sv->active[k]->id == job_id) {
+            std::unique_ptr<Job> jp = std::move(sv->active[k]);
+            sv->active.erase(sv->active.begin() + (std::ptrdiff_t)k);
+            if (jp->form == 1) {   // its state is read on its own stream, after the packed work queued
+                cudaEventRecord(sv->pk_tail, sv->pstream);
+                cudaStreamWaitEvent(jp->ctx->c.stream, sv->pk_tail, 0);
+            }
+            server_record(sv, *jp, ERP_ECANCELED);
+            // the rounds launched so far may still run its kernels: its context goes
+            // (and its budget returns) once the last of them has completed
+            sv->grave.emplace_back(sv->rounds_launched, std::move(jp));
+            return ERP_OK;
+        }
+    for (auto &jp : sv->preparing)   // being set up: retired when its worker is done
+        if (jp->id == job_id) {
+            jp->cancel = true;
+            return ERP_OK;
+        }
+    sv->err = "no queued or running job with id " + std::to_string(job_id);
+    return ERP_EINVAL;
 }
 
 extern "C" erp_status erp_server_poll(erp_server *sv, erp_job_result *out, int32_t cap, int32_t *count) {

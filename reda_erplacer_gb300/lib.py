@@ -15,7 +15,7 @@ LIB_PATH = os.environ.get("ERP_LIBRARY") or os.path.join(HERE, "liberplacer_gb30
 f32p = C.POINTER(C.c_float)
 i32p = C.POINTER(C.c_int32)
 
-OK, EINVAL, ENOMEM, ECUDA, ENAN, ETIMEDOUT, ENOTSUP, ENODEV, ESTATE = range(9)
+OK, EINVAL, ENOMEM, ECUDA, ENAN, ETIMEDOUT, ENOTSUP, ENODEV, ESTATE, ECANCELED = range(10)
 START_CENTER, START_DB = 0, 1
 STAGES = ("wirelength", "wl_gather", "density", "spectral", "force", "nesterov", "scheduler")
 PREC_FP32, PREC_TF32_GEMM, PREC_BF16X3_GEMM = 0, 1, 2
@@ -112,6 +112,7 @@ EXPORTS = {
     "erp_server_create": (C.c_int, [C.POINTER(ServerParams), C.POINTER(C.c_void_p)]),
     "erp_server_submit": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(Design), C.POINTER(Params)]),
     "erp_server_pump": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "erp_server_cancel": (C.c_int, [C.c_void_p, C.c_int64]),
     "erp_server_poll": (C.c_int, [C.c_void_p, C.POINTER(JobResult), C.c_int32, C.POINTER(C.c_int32)]),
     "erp_server_positions": (C.c_int, [C.c_void_p, C.c_int64, f32p, f32p]),
     "erp_server_now": (C.c_double, [C.c_void_p]),

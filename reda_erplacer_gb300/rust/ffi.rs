@@ -13,6 +13,7 @@ use std::os::raw::{c_char, c_int, c_void};
 pub type erp_status = c_int;
 pub const ERP_OK: erp_status = 0;
 pub const ERP_ETIMEDOUT: erp_status = 5;
+pub const ERP_ECANCELED: erp_status = 9;
 
 pub const ERP_START_CENTER: i32 = 0; // src/placement.rs:109-139
 pub const ERP_START_DB: i32 = 1;
@@ -240,6 +241,7 @@ extern "C" {
     pub fn erp_server_submit(s: *mut erp_server, job_id: i64, d: *const erp_design,
                              p: *const erp_params) -> erp_status;
     pub fn erp_server_pump(s: *mut erp_server, active: *mut i32, queued: *mut i32) -> erp_status;
+    pub fn erp_server_cancel(s: *mut erp_server, job_id: i64) -> erp_status;
     pub fn erp_server_poll(s: *mut erp_server, out: *mut erp_job_result, cap: i32, count: *mut i32) -> erp_status;
     pub fn erp_server_positions(s: *mut erp_server, job_id: i64, x: *mut f32, y: *mut f32) -> erp_status;
     pub fn erp_server_now(s: *const erp_server) -> f64;

@@ -36,6 +36,11 @@ class Server:
         self._ck(self.lib.erp_server_pump(self.h, C.byref(a), C.byref(q)))
         return a.value, q.value
 
+    def cancel(self, job_id):
+        """Withdraw a queued or running job (erp_server_cancel); its result
+        carries ECANCELED."""
+        self._ck(self.lib.erp_server_cancel(self.h, int(job_id)))
+
     def poll(self):
         buf = (JobResult * 256)()
         out = []

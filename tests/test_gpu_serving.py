@@ -76,3 +76,45 @@ def test_server_admission_by_footprint(R):
     res = run_stream(sv, jobs[:1], np.zeros(1))
     assert res[0]["status"] == R.lib.ENOMEM
     sv.close()
+
+
+def test_server_cancel(R):
+    """A queued job and a running job withdrawn mid-stream report ECANCELED and
+    free their slot; every other job ends with the results it has alone."""
+    from reda_erplacer_gb300.serving import Server
+    jobs = _jobs(R, 8, seed=93)
+    sv = Server(max_active=3, hbm_budget_gb=8.0, max_iterations=80, stop_overflow=0.0, chunk=8,
+                keep_positions=True)
+    for i, (d, b) in enumerate(jobs):
+        sv.submit(i, d, b)
+    res = []
+    for _ in range(4):   # a few rounds: some jobs running, the rest queued
+        sv.pump()
+        res += sv.poll()
+    sv.cancel(7)                             # still queued (three slots, FIFO)
+    running = [j for j in range(7) if j not in {r["job_id"] for r in res}][0]
+    sv.cancel(running)
+    with pytest.raises(R.lib.ErpError) as e:
+        sv.cancel(12345)
+    assert e.value.status == R.lib.EINVAL
+    while True:
+        active, queued = sv.pump()
+        res += sv.poll()
+        if not active and not queued:
+            break
+    res += sv.poll()
+    by_id = {r["job_id"]: r for r in res}
+    assert sorted(by_id) == list(range(8))
+    assert by_id[7]["status"] == R.lib.ECANCELED and by_id[7]["iterations"] == 0
+    assert by_id[running]["status"] == R.lib.ECANCELED and by_id[running]["iterations"] < 80
+    for i, (d, b) in enumerate(jobs):
+        if i in (7, running):
+            continue
+        assert by_id[i]["status"] == 0 and by_id[i]["iterations"] == 80
+        pl = R.Placement(d, b, 1.0, start_mode=1)
+        pl.run(80)
+        xa, ya = pl.positions()
+        xb, yb = sv.positions(i)
+        assert np.array_equal(xa, xb) and np.array_equal(ya, yb), i
+        pl.close()
+    sv.close()
